@@ -1,0 +1,832 @@
+// The C ABI of gbnuts: model handles (the model_base stand-in), the batched
+// gradient entry points, the device run loop and the two sampling services
+// with the reference's writer / logger / interrupt protocol.
+//
+// Service protocol restated from (paths relative to the stan-dev/stan tree):
+//   src/stan/services/sample/hmc_nuts_diag_e_adapt.hpp:331-407 (set-up, error codes)
+//   src/stan/services/sample/hmc_nuts_diag_e.hpp:48-100
+//   src/stan/services/util/run_adaptive_sampler.hpp:46-103, run_sampler.hpp
+//   src/stan/services/util/mcmc_writer.hpp:63-259 (names, rows, adaptation, timing)
+//   src/stan/mcmc/windowed_adaptation.hpp:29-78 (set_window_params and its messages)
+//   src/stan/services/util/initialize.hpp:68-227 (init messages)
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/gbnuts.h"
+#include "gbnuts_internal.h"
+#include "nuts_device.h"
+
+namespace gbn {
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& s) { g_last_error = s; }
+const std::string& last_error() { return g_last_error; }
+}  // namespace gbn
+
+using namespace gbn;
+
+struct gbnuts_model {
+  ModelDesc desc;
+  void* d_X = nullptr;
+  double* d_y = nullptr;
+  int* d_group = nullptr;
+  std::vector<int> h_group_off;  // J+1
+  // single-point and batch scratch (owned by the handle)
+  GradWorkspace ws;
+  double* d_theta = nullptr;
+  double* d_lp = nullptr;
+  double* d_grad = nullptr;
+  int scratch_C = 0;
+  cudaStream_t stream = nullptr;
+};
+
+static int fail(int code, const std::string& msg) {
+  set_last_error(msg);
+  return code;
+}
+
+static void host_names(const ModelDesc& m, bool constrained_unused, std::vector<std::string>& out) {
+  (void)constrained_unused;
+  out.clear();
+  if (m.kind == GBNUTS_LOGISTIC || m.kind == GBNUTS_POISSON) {
+    if (m.has_base) out.push_back("alpha");
+  } else if (m.kind == GBNUTS_HIER_NORMAL) {
+    out.push_back("mu");
+    out.push_back("tau");
+    out.push_back("sigma");
+  } else {
+    out.push_back("alpha");
+    out.push_back("tau");
+  }
+  for (int j = 0; j < (m.off_z >= 0 ? m.J : 0); ++j) out.push_back("z." + std::to_string(j + 1));
+  for (int k = 0; k < m.K; ++k) out.push_back("beta." + std::to_string(k + 1));
+}
+
+static int ensure_scratch(gbnuts_model* m, int C) {
+  if (m->scratch_C >= C) return GBNUTS_OK;
+  if (m->d_theta) cudaFree(m->d_theta);
+  m->d_theta = nullptr;
+  const size_t D = m->desc.D;
+  char* base = nullptr;
+  GBN_CUDA_TRY(cudaMalloc(&base, (size_t)C * (2 * D + 1) * sizeof(double)));
+  m->d_theta = reinterpret_cast<double*>(base);
+  m->d_grad = m->d_theta + (size_t)C * D;
+  m->d_lp = m->d_grad + (size_t)C * D;
+  m->scratch_C = C;
+  return GBNUTS_OK;
+}
+
+extern "C" {
+
+int gbnuts_last_error(char* buf, int cap) {
+  if (!buf || cap <= 0) return -1;
+  strncpy(buf, g_last_error.c_str(), cap - 1);
+  buf[cap - 1] = 0;
+  return (int)g_last_error.size();
+}
+
+int gbnuts_device_info(char* buf, int cap) {
+  int dev = 0, rt = 0, drv = 0;
+  cudaDeviceProp p;
+  std::ostringstream s;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&p, dev) != cudaSuccess) {
+    s << "no CUDA device";
+  } else {
+    cudaRuntimeGetVersion(&rt);
+    cudaDriverGetVersion(&drv);
+    s << p.name << " sm_" << p.major << p.minor << " SMs=" << p.multiProcessorCount
+      << " runtime=" << rt << " driver=" << drv;
+  }
+  std::string str = s.str();
+  if (buf && cap > 0) {
+    strncpy(buf, str.c_str(), cap - 1);
+    buf[cap - 1] = 0;
+  }
+  return (int)str.size();
+}
+
+int gbnuts_model_create(int kind, const void* X, int x_dtype, const double* y,
+                        const int* group, long long N, int K, int J, int intercept,
+                        const double* hp, int n_hp, gbnuts_model** out) {
+  if (!out) return fail(GBNUTS_USAGE, "out is NULL");
+  *out = nullptr;
+  if (kind < GBNUTS_LOGISTIC || kind > GBNUTS_HIER_LOGISTIC)
+    return fail(GBNUTS_USAGE, "unknown model kind");
+  if (x_dtype < GBNUTS_F64 || x_dtype > GBNUTS_BF16) return fail(GBNUTS_USAGE, "unknown x_dtype");
+  if (N <= 0 || K < 0 || (K > 0 && !X) || !y) return fail(GBNUTS_DATAERR, "bad data shape");
+  if (chains_per_block(K) == 0) return fail(GBNUTS_USAGE, "K above 2048 is not supported");
+  const bool hier = kind == GBNUTS_HIER_NORMAL || kind == GBNUTS_HIER_LOGISTIC;
+  if (hier && (J <= 0 || !group)) return fail(GBNUTS_DATAERR, "hierarchical model needs J > 0 and group");
+  // data checks (DATAERR): finite X and y, valid 0/1 or count y, sorted groups
+  const size_t NK = (size_t)N * K;
+  for (size_t i = 0; i < NK; ++i) {
+    double v;
+    if (x_dtype == GBNUTS_F64)
+      v = static_cast<const double*>(X)[i];
+    else if (x_dtype == GBNUTS_F32)
+      v = static_cast<const float*>(X)[i];
+    else {
+      uint32_t b = ((uint32_t) static_cast<const uint16_t*>(X)[i]) << 16;
+      float f;
+      memcpy(&f, &b, 4);
+      v = f;
+    }
+    if (!isfinite(v)) return fail(GBNUTS_DATAERR, "X has a non-finite value");
+  }
+  double sum_lgamma = 0.0;
+  for (long long n = 0; n < N; ++n) {
+    double v = y[n];
+    if (!isfinite(v)) return fail(GBNUTS_DATAERR, "y has a non-finite value");
+    if ((kind == GBNUTS_LOGISTIC || kind == GBNUTS_HIER_LOGISTIC) && v != 0.0 && v != 1.0)
+      return fail(GBNUTS_DATAERR, "logistic y must be 0 or 1");
+    if (kind == GBNUTS_POISSON) {
+      if (v < 0 || v != floor(v)) return fail(GBNUTS_DATAERR, "Poisson y must be counts");
+      sum_lgamma += lgamma(v + 1.0);
+    }
+  }
+  std::vector<int> off;
+  if (hier) {
+    off.assign(J + 1, 0);
+    int prev = -1;
+    for (long long n = 0; n < N; ++n) {
+      int g = group[n];
+      if (g < 0 || g >= J) return fail(GBNUTS_DATAERR, "group index out of range");
+      if (g < prev) return fail(GBNUTS_DATAERR, "rows must be sorted by group");
+      prev = g;
+      off[g + 1]++;
+    }
+    for (int j = 0; j < J; ++j) off[j + 1] += off[j];
+  }
+  gbnuts_model* m = new gbnuts_model();
+  ModelDesc& d = m->desc;
+  memset(&d, 0, sizeof(d));
+  d.kind = kind;
+  d.N = N;
+  d.K = K;
+  d.J = hier ? J : 0;
+  d.x_dtype = x_dtype;
+  d.idx_tau = d.idx_sigma = d.off_z = -1;
+  auto hpv = [&](int i, double dflt) { return (hp && i < n_hp) ? hp[i] : dflt; };
+  switch (kind) {
+    case GBNUTS_LOGISTIC:
+    case GBNUTS_POISSON:
+      d.link = kind == GBNUTS_LOGISTIC ? LINK_LOGIT : LINK_POISSON_LOG;
+      d.has_base = intercept ? 1 : 0;
+      d.off_beta = d.has_base;
+      d.D = K + d.has_base;
+      d.s_base = d.s_beta = hpv(0, kind == GBNUTS_LOGISTIC ? 2.5 : 1.0);
+      break;
+    case GBNUTS_HIER_NORMAL:
+      d.link = LINK_NORMAL;
+      d.has_base = 1;
+      d.idx_tau = 1;
+      d.idx_sigma = 2;
+      d.off_z = 3;
+      d.off_beta = 3 + J;
+      d.D = 3 + J + K;
+      d.s_base = hpv(0, 5.0);
+      d.s_tau = hpv(1, 1.0);
+      d.s_sigma = hpv(2, 1.0);
+      d.s_beta = hpv(3, 1.0);
+      break;
+    default:
+      d.link = LINK_LOGIT;
+      d.has_base = 1;
+      d.idx_tau = 1;
+      d.off_z = 2;
+      d.off_beta = 2 + J;
+      d.D = 2 + J + K;
+      d.s_base = hpv(0, 2.5);
+      d.s_tau = hpv(1, 1.0);
+      d.s_beta = hpv(2, 2.5);
+      break;
+  }
+  d.sum_lgamma_y = sum_lgamma;
+  const size_t xbytes = NK * (x_dtype == GBNUTS_F64 ? 8 : x_dtype == GBNUTS_F32 ? 4 : 2);
+  cudaError_t e = cudaSuccess;
+  if (xbytes) e = cudaMalloc(&m->d_X, xbytes);
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_y, N * sizeof(double));
+  if (e == cudaSuccess && hier) e = cudaMalloc(&m->d_group, N * sizeof(int));
+  if (e == cudaSuccess && xbytes) e = cudaMemcpy(m->d_X, X, xbytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->d_y, y, N * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && hier)
+    e = cudaMemcpy(m->d_group, group, N * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    gbnuts_model_destroy(m);
+    return fail(GBNUTS_SOFTWARE, std::string("device allocation: ") + cudaGetErrorString(e));
+  }
+  d.X = m->d_X;
+  d.y = m->d_y;
+  d.group = m->d_group;
+  m->h_group_off = off;
+  *out = m;
+  return GBNUTS_OK;
+}
+
+void gbnuts_model_destroy(gbnuts_model* m) {
+  if (!m) return;
+  free_workspace(m->ws);
+  if (m->d_theta) cudaFree(m->d_theta);
+  if (m->d_X) cudaFree(m->d_X);
+  if (m->d_y) cudaFree(m->d_y);
+  if (m->d_group) cudaFree(m->d_group);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+}
+
+int gbnuts_num_params_r(const gbnuts_model* m) { return m ? m->desc.D : -1; }
+
+int gbnuts_param_name(const gbnuts_model* m, int index, int constrained, char* buf, int cap) {
+  if (!m || index < 0 || index >= m->desc.D) return -1;
+  std::vector<std::string> names;
+  host_names(m->desc, constrained != 0, names);
+  const std::string& s = names[index];
+  if (buf && cap > 0) {
+    strncpy(buf, s.c_str(), cap - 1);
+    buf[cap - 1] = 0;
+  }
+  return (int)s.size();
+}
+
+static int eval_points(gbnuts_model* m, int C, const double* theta, int propto, int jacobian,
+                       double* lp, double* grad, int precision) {
+  if (!m || C <= 0 || !theta) return fail(GBNUTS_USAGE, "bad arguments");
+  const int D = m->desc.D;
+  int rc = ensure_scratch(m, C);
+  if (rc) return rc;
+  rc = prepare_workspace(m->desc, m->h_group_off.data(), C, precision, m->ws);
+  if (rc) return rc;
+  GBN_CUDA_TRY(cudaMemcpyAsync(m->d_theta, theta, (size_t)C * D * sizeof(double),
+                               cudaMemcpyHostToDevice, m->stream));
+  rc = launch_log_prob_grad(m->desc, precision, m->d_theta, D, C, nullptr, m->d_lp, m->d_grad,
+                            D, propto, jacobian, m->ws, m->stream, nullptr, nullptr);
+  if (rc) return rc;
+  GBN_CUDA_TRY(cudaMemcpyAsync(lp, m->d_lp, C * sizeof(double), cudaMemcpyDeviceToHost,
+                               m->stream));
+  if (grad)
+    GBN_CUDA_TRY(cudaMemcpyAsync(grad, m->d_grad, (size_t)C * D * sizeof(double),
+                                 cudaMemcpyDeviceToHost, m->stream));
+  GBN_CUDA_TRY(cudaStreamSynchronize(m->stream));
+  return GBNUTS_OK;
+}
+
+int gbnuts_log_prob(gbnuts_model* m, const double* theta, int propto, int jacobian,
+                    double* lp) {
+  if (!lp) return fail(GBNUTS_USAGE, "lp is NULL");
+  return eval_points(m, 1, theta, propto, jacobian, lp, nullptr, GBNUTS_PREC_FP64);
+}
+
+int gbnuts_log_prob_grad(gbnuts_model* m, const double* theta, int propto, int jacobian,
+                         double* lp, double* grad) {
+  if (!lp || !grad) return fail(GBNUTS_USAGE, "lp or grad is NULL");
+  return eval_points(m, 1, theta, propto, jacobian, lp, grad, GBNUTS_PREC_FP64);
+}
+
+int gbnuts_log_prob_grad_batch(gbnuts_model* m, int C, const double* theta, double* lp,
+                               double* grad, int precision) {
+  if (!lp || !grad) return fail(GBNUTS_USAGE, "lp or grad is NULL");
+  return eval_points(m, C, theta, 1, 1, lp, grad, precision);
+}
+
+int gbnuts_log_prob_grad_batch_device(gbnuts_model* m, int C, const double* d_theta,
+                                      double* d_lp, double* d_grad, int precision,
+                                      void* stream) {
+  if (!m || C <= 0 || !d_theta || !d_lp || !d_grad) return fail(GBNUTS_USAGE, "bad arguments");
+  int rc = prepare_workspace(m->desc, m->h_group_off.data(), C, precision, m->ws);
+  if (rc) return rc;
+  return launch_log_prob_grad(m->desc, precision, d_theta, m->desc.D, C, nullptr, d_lp, d_grad,
+                              m->desc.D, 1, 1, m->ws, static_cast<cudaStream_t>(stream),
+                              nullptr, nullptr);
+}
+
+int gbnuts_write_array(const gbnuts_model* m, const double* th, double* out) {
+  if (!m || !th || !out) return fail(GBNUTS_USAGE, "bad arguments");
+  for (int d = 0; d < m->desc.D; ++d) {
+    double v = th[d];
+    if (d == m->desc.idx_tau || d == m->desc.idx_sigma) v = exp(v);
+    out[d] = v;
+  }
+  return GBNUTS_OK;
+}
+
+int gbnuts_unconstrain_array(const gbnuts_model* m, const double* th, double* out) {
+  if (!m || !th || !out) return fail(GBNUTS_USAGE, "bad arguments");
+  for (int d = 0; d < m->desc.D; ++d) {
+    double v = th[d];
+    if (d == m->desc.idx_tau || d == m->desc.idx_sigma) {
+      if (!(v > 0)) return fail(GBNUTS_DATAERR, "positive parameter is not positive");
+      v = log(v);
+    }
+    out[d] = v;
+  }
+  return GBNUTS_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ the run
+namespace {
+
+struct WindowParams {
+  unsigned num_warmup = 0, init_buffer = 0, term_buffer = 0, base_window = 0;
+  unsigned size0 = 0, next0 = 0;
+  std::vector<std::string> messages;
+};
+
+// windowed_adaptation::set_window_params (windowed_adaptation.hpp:29-78), on
+// a freshly constructed adapter whose restart() left size 0 and end index
+// 0 + 0 - 1 (unsigned).
+WindowParams window_params(unsigned nw, unsigned ib, unsigned tb, unsigned bw) {
+  WindowParams w;
+  w.size0 = 0;
+  w.next0 = 0u + 0u - 1u;
+  if (nw < 20) {
+    w.messages = {"WARNING: No variance estimation is", "         performed for num_warmup < 20",
+                  ""};
+    return w;
+  }
+  if (ib + bw + tb > nw) {
+    w.num_warmup = nw;
+    w.init_buffer = (unsigned)(0.15 * nw);
+    w.term_buffer = (unsigned)(0.1 * nw);
+    w.base_window = nw - (w.init_buffer + w.term_buffer);
+    std::ostringstream a, b, c;
+    a << "           init_buffer = " << w.init_buffer;
+    b << "           adapt_window = " << w.base_window;
+    c << "           term_buffer = " << w.term_buffer;
+    w.messages = {"WARNING: There aren't enough warmup iterations to fit the",
+                  "         three stages of adaptation as currently configured.",
+                  "         Reducing each adaptation stage to 15%/75%/10% of",
+                  "         the given number of warmup iterations:",
+                  a.str(), b.str(), c.str(), ""};
+    return w;
+  }
+  w.num_warmup = nw;
+  w.init_buffer = ib;
+  w.term_buffer = tb;
+  w.base_window = bw;
+  w.size0 = bw;
+  w.next0 = ib + bw - 1u;
+  return w;
+}
+
+struct DeviceRun {
+  std::vector<void*> allocs;
+  ~DeviceRun() {
+    for (void* p : allocs) cudaFree(p);
+  }
+  template <typename T>
+  cudaError_t alloc(T** p, size_t n) {
+    void* v = nullptr;
+    cudaError_t e = cudaMalloc(&v, std::max<size_t>(n, 1) * sizeof(T));
+    if (e == cudaSuccess) allocs.push_back(v);
+    *p = static_cast<T*>(v);
+    return e;
+  }
+};
+
+}  // namespace
+
+extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
+                                 gbnuts_run_output* out, const gbnuts_callbacks* cb) {
+  if (!m || !rc || !out) return fail(GBNUTS_USAGE, "bad arguments");
+  const int C = rc->num_chains;
+  const int D = m->desc.D;
+  if (C <= 0) return fail(GBNUTS_USAGE, "num_chains must be positive");
+  if (rc->num_warmup < 0 || rc->num_samples < 0) return fail(GBNUTS_USAGE, "negative iterations");
+  if (rc->num_thin < 1) return fail(GBNUTS_USAGE, "num_thin must be at least 1");
+  if (!out->draws || !out->n_rows) return fail(GBNUTS_USAGE, "draws / n_rows buffers missing");
+  // base_nuts::set_max_depth ignores non-positive depths (default 5)
+  const int max_depth = rc->max_depth > 0 ? rc->max_depth : 5;
+  if (max_depth > MAX_TREE_DEPTH) return fail(GBNUTS_USAGE, "max_depth above 16 is not supported");
+  if (rc->inv_metrics) {
+    for (size_t i = 0; i < (size_t)C * D; ++i)
+      if (!isfinite(rc->inv_metrics[i]) || !(rc->inv_metrics[i] > 0))
+        return fail(GBNUTS_CONFIG, "Inverse Euclidean metric not positive definite.");
+  }
+  const int n_cols = 7 + D;
+  const int warm_rows = rc->save_warmup ? (rc->num_warmup + rc->num_thin - 1) / rc->num_thin : 0;
+  const int samp_rows = (rc->num_samples + rc->num_thin - 1) / rc->num_thin;
+  const int need_rows = warm_rows + samp_rows;
+  if (out->max_rows < need_rows || out->n_cols != n_cols)
+    return fail(GBNUTS_USAGE, "output buffer too small (max_rows / n_cols)");
+
+  SamplerCfg cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.C = C;
+  cfg.D = D;
+  cfg.ld = (D + 3) & ~3;
+  cfg.max_depth = max_depth;
+  cfg.n_slots = SL_STACK + 6 * max_depth;
+  cfg.adapt = rc->adapt ? 1 : 0;
+  cfg.num_warmup = rc->num_warmup;
+  cfg.num_samples = rc->num_samples;
+  cfg.num_thin = rc->num_thin;
+  cfg.save_warmup = rc->save_warmup ? 1 : 0;
+  cfg.max_rows = out->max_rows;
+  cfg.n_cols = n_cols;
+  cfg.stepsize = rc->stepsize > 0 ? rc->stepsize : 0.1;  // set_nominal_stepsize ignores e <= 0
+  cfg.jitter = (rc->stepsize_jitter > 0 && rc->stepsize_jitter < 1) ? rc->stepsize_jitter : 0.0;
+  // stepsize_adaptation setters keep their defaults for invalid values
+  cfg.delta = (rc->delta > 0 && rc->delta < 1) ? rc->delta : 0.5;
+  cfg.gamma = rc->gamma > 0 ? rc->gamma : 0.05;
+  cfg.kappa = rc->kappa > 0 ? rc->kappa : 0.75;
+  cfg.t0 = rc->t0 > 0 ? rc->t0 : 10;
+  cfg.init_radius = rc->init_radius;
+  cfg.seed = rc->random_seed;
+  cfg.init_chain_id = rc->init_chain_id;
+  cfg.idx_tau = m->desc.idx_tau;
+  cfg.idx_sigma = m->desc.idx_sigma;
+  WindowParams wp = window_params(rc->num_warmup, rc->init_buffer, rc->term_buffer, rc->window);
+  if (rc->adapt) {
+    cfg.wa_num_warmup = wp.num_warmup;
+    cfg.wa_init_buffer = wp.init_buffer;
+    cfg.wa_term_buffer = wp.term_buffer;
+    cfg.wa_base_window = wp.base_window;
+    cfg.wa_size0 = wp.size0;
+    cfg.wa_next0 = wp.next0;
+    if (cb && cb->log)
+      for (int c = 0; c < C; ++c)
+        for (auto& s : wp.messages) cb->log(cb->ctx, GBNUTS_INFO, s.c_str());
+  }
+
+  cudaStream_t st = m->stream;
+  DeviceRun dr;
+  ChainState* d_states;
+  double *d_vecs, *d_req, *d_lp, *d_grad, *d_draws, *d_diag = nullptr, *d_init, *d_inits = nullptr,
+                                                   *d_invm = nullptr;
+  int *d_active, *d_done, *d_abort;
+  GBN_CUDA_TRY(dr.alloc(&d_states, C));
+  GBN_CUDA_TRY(dr.alloc(&d_vecs, (size_t)C * cfg.n_slots * cfg.ld));
+  GBN_CUDA_TRY(dr.alloc(&d_req, (size_t)C * cfg.ld));
+  GBN_CUDA_TRY(dr.alloc(&d_grad, (size_t)C * cfg.ld));
+  GBN_CUDA_TRY(dr.alloc(&d_lp, C));
+  GBN_CUDA_TRY(dr.alloc(&d_active, C));
+  GBN_CUDA_TRY(dr.alloc(&d_draws, (size_t)C * out->max_rows * n_cols));
+  if (out->diagnostics) GBN_CUDA_TRY(dr.alloc(&d_diag, (size_t)C * out->max_rows * 3 * D));
+  GBN_CUDA_TRY(dr.alloc(&d_init, (size_t)C * D));
+  GBN_CUDA_TRY(dr.alloc(&d_done, 1));
+  GBN_CUDA_TRY(dr.alloc(&d_abort, 1));
+  if (rc->inits) {
+    GBN_CUDA_TRY(dr.alloc(&d_inits, (size_t)C * D));
+    GBN_CUDA_TRY(cudaMemcpyAsync(d_inits, rc->inits, (size_t)C * D * sizeof(double),
+                                 cudaMemcpyHostToDevice, st));
+  }
+  if (rc->inv_metrics) {
+    GBN_CUDA_TRY(dr.alloc(&d_invm, (size_t)C * D));
+    GBN_CUDA_TRY(cudaMemcpyAsync(d_invm, rc->inv_metrics, (size_t)C * D * sizeof(double),
+                                 cudaMemcpyHostToDevice, st));
+  }
+  GBN_CUDA_TRY(cudaMemsetAsync(d_done, 0, sizeof(int), st));
+  GBN_CUDA_TRY(cudaMemsetAsync(d_abort, 0, sizeof(int), st));
+  GBN_CUDA_TRY(cudaMemsetAsync(d_grad, 0, (size_t)C * cfg.ld * sizeof(double), st));
+  GBN_CUDA_TRY(cudaMemsetAsync(d_draws, 0, (size_t)C * out->max_rows * n_cols * sizeof(double), st));
+  int prc = prepare_workspace(m->desc, m->h_group_off.data(), C, rc->precision, m->ws);
+  if (prc) return prc;
+
+  int* h_done = nullptr;
+  GBN_CUDA_TRY(cudaMallocHost(&h_done, sizeof(int)));
+  struct PinnedGuard {
+    int* p;
+    ~PinnedGuard() { cudaFreeHost(p); }
+  } pg{h_done};
+
+  cudaEvent_t ev_begin, ev_end;
+  GBN_CUDA_TRY(cudaEventCreate(&ev_begin));
+  GBN_CUDA_TRY(cudaEventCreate(&ev_end));
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> grad_events;
+  const int kSampleEvery = 16;
+  const size_t kMaxSamples = 512;
+
+  launch_nuts_init(cfg, d_states, d_vecs, d_invm, d_active, d_lp, st);
+  GBN_CUDA_TRY(cudaGetLastError());
+  GBN_CUDA_TRY(cudaEventRecord(ev_begin, st));
+  auto wall0 = std::chrono::steady_clock::now();
+
+  long long step = 0;
+  const int chunk = 32;
+  // upper bound on steps: every transition is at most 2^max_depth - 1 leapfrogs,
+  // step-size searches are bounded by the 1e7 / 0 stops, 100 init tries.
+  const long long iters = (long long)rc->num_warmup + rc->num_samples;
+  const long long max_steps = (iters + 2) * ((1LL << max_depth) + 200) + 1000;
+  int status_rc = GBNUTS_OK;
+  long long launches = 0;
+  for (;;) {
+    for (int k = 0; k < chunk; ++k) {
+      launch_nuts_step(cfg, d_states, d_vecs, d_req, d_lp, d_grad, d_active, d_draws, d_diag,
+                       d_init, d_inits, d_done, d_abort, step, st);
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      if ((step % kSampleEvery) == 0 && grad_events.size() < kMaxSamples) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        grad_events.emplace_back(e0, e1);
+      }
+      int r = launch_log_prob_grad(m->desc, rc->precision, d_req, cfg.ld, C, d_active, d_lp,
+                                   d_grad, cfg.ld, 1, 1, m->ws, st, e0, e1);
+      if (r) return r;
+      launches += 2 + (m->desc.off_z >= 0 ? 1 : 0) + 1;
+      ++step;
+    }
+    GBN_CUDA_TRY(cudaMemcpyAsync(h_done, d_done, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GBN_CUDA_TRY(cudaStreamSynchronize(st));
+    if (*h_done >= C) break;
+    if (cb && cb->interrupt && cb->interrupt(cb->ctx)) {
+      int one = 1;
+      GBN_CUDA_TRY(cudaMemcpyAsync(d_abort, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+    }
+    if (step > max_steps) {
+      status_rc = fail(GBNUTS_SOFTWARE, "device run exceeded its step bound");
+      break;
+    }
+  }
+  GBN_CUDA_TRY(cudaEventRecord(ev_end, st));
+  GBN_CUDA_TRY(cudaStreamSynchronize(st));
+  auto wall1 = std::chrono::steady_clock::now();
+  float total_ms = 0;
+  cudaEventElapsedTime(&total_ms, ev_begin, ev_end);
+  double grad_ms_sum = 0;
+  int grad_n = 0;
+  for (auto& pr : grad_events) {
+    float t = 0;
+    if (cudaEventElapsedTime(&t, pr.first, pr.second) == cudaSuccess) {
+      grad_ms_sum += t;
+      ++grad_n;
+    }
+    cudaEventDestroy(pr.first);
+    cudaEventDestroy(pr.second);
+  }
+  cudaEventDestroy(ev_begin);
+  cudaEventDestroy(ev_end);
+
+  std::vector<ChainState> hs(C);
+  GBN_CUDA_TRY(cudaMemcpy(hs.data(), d_states, C * sizeof(ChainState), cudaMemcpyDeviceToHost));
+  GBN_CUDA_TRY(cudaMemcpy(out->draws, d_draws, (size_t)C * out->max_rows * n_cols * sizeof(double),
+                          cudaMemcpyDeviceToHost));
+  if (out->diagnostics && d_diag)
+    GBN_CUDA_TRY(cudaMemcpy(out->diagnostics, d_diag,
+                            (size_t)C * out->max_rows * 3 * D * sizeof(double),
+                            cudaMemcpyDeviceToHost));
+  if (out->init)
+    GBN_CUDA_TRY(cudaMemcpy(out->init, d_init, (size_t)C * D * sizeof(double),
+                            cudaMemcpyDeviceToHost));
+  if (out->inv_metric)
+    GBN_CUDA_TRY(cudaMemcpy2D(out->inv_metric, D * sizeof(double),
+                              d_vecs + (size_t)SL_INVM * cfg.ld,
+                              (size_t)cfg.n_slots * cfg.ld * sizeof(double), D * sizeof(double),
+                              C, cudaMemcpyDeviceToHost));
+  const double wall_s = std::chrono::duration<double>(wall1 - wall0).count();
+  for (int c = 0; c < C; ++c) {
+    out->n_rows[c] = hs[c].rows;
+    if (out->n_warmup_rows) out->n_warmup_rows[c] = hs[c].warm_rows;
+    if (out->status) out->status[c] = hs[c].status;
+    if (out->stepsize) out->stepsize[c] = hs[c].nom_eps;
+    if (out->n_grad) out->n_grad[c] = hs[c].n_grad;
+    if (out->seconds) {
+      double frac = (hs[c].warm_end_step >= 0 && step > 0) ? (double)hs[c].warm_end_step / step : 0.0;
+      out->seconds[2 * c] = wall_s * frac;
+      out->seconds[2 * c + 1] = wall_s * (1.0 - frac);
+    }
+  }
+  out->total_ms = total_ms;
+  out->grad_ms = grad_n ? grad_ms_sum / grad_n : 0.0;
+  out->steps = step;
+  out->kernel_launches = launches;
+  return status_rc;
+}
+
+// ------------------------------------------------------------------ services
+namespace {
+
+std::string fmt(double v) {
+  std::ostringstream s;
+  s << v;
+  return s.str();
+}
+
+void emit_msg(const gbnuts_callbacks* cb, int c, int w, const std::string& s) {
+  if (cb && cb->write_message) cb->write_message(cb->ctx, c, w, s.c_str());
+}
+void emit_blank(const gbnuts_callbacks* cb, int c, int w) {
+  if (cb && cb->write_blank) cb->write_blank(cb->ctx, c, w);
+}
+void emit_log(const gbnuts_callbacks* cb, int level, const std::string& s) {
+  if (cb && cb->log) cb->log(cb->ctx, level, s.c_str());
+}
+void emit_names(const gbnuts_callbacks* cb, int c, int w, const std::vector<std::string>& v) {
+  if (!cb || !cb->write_names) return;
+  std::vector<const char*> p;
+  for (auto& s : v) p.push_back(s.c_str());
+  cb->write_names(cb->ctx, c, w, p.data(), (int)p.size());
+}
+void emit_values(const gbnuts_callbacks* cb, int c, int w, const double* v, int n) {
+  if (cb && cb->write_values) cb->write_values(cb->ctx, c, w, v, n);
+}
+
+// mcmc_writer::write_timing (mcmc_writer.hpp:198-218) to one writer
+void write_timing(const gbnuts_callbacks* cb, int c, int w, double warm, double samp) {
+  const std::string title(" Elapsed Time: ");
+  emit_blank(cb, c, w);
+  emit_msg(cb, c, w, title + fmt(warm) + " seconds (Warm-up)");
+  emit_msg(cb, c, w, std::string(title.size(), ' ') + fmt(samp) + " seconds (Sampling)");
+  emit_msg(cb, c, w, std::string(title.size(), ' ') + fmt(warm + samp) + " seconds (Total)");
+  emit_blank(cb, c, w);
+}
+
+int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* cb) {
+  const int C = rc.num_chains, D = m ? m->desc.D : 0;
+  if (!m || C <= 0) return fail(GBNUTS_USAGE, "bad arguments");
+  const int n_cols = 7 + D;
+  const int thin = std::max(1, rc.num_thin);
+  const int rows = (rc.save_warmup ? (rc.num_warmup + thin - 1) / thin : 0) +
+                   (rc.num_samples + thin - 1) / thin;
+  const bool diag = cb && cb->want_diagnostics;
+  std::vector<double> draws((size_t)C * std::max(rows, 1) * n_cols), dg;
+  if (diag) dg.resize((size_t)C * std::max(rows, 1) * 3 * D);
+  std::vector<int> n_rows(C), n_warm(C), status(C);
+  std::vector<double> eps(C), invm((size_t)C * D), init((size_t)C * D), secs(2 * C);
+  std::vector<long long> ngrad(C);
+  gbnuts_run_output o;
+  memset(&o, 0, sizeof(o));
+  o.max_rows = std::max(rows, 1);
+  o.n_cols = n_cols;
+  o.draws = draws.data();
+  o.diagnostics = diag ? dg.data() : nullptr;
+  o.n_rows = n_rows.data();
+  o.n_warmup_rows = n_warm.data();
+  o.status = status.data();
+  o.stepsize = eps.data();
+  o.inv_metric = invm.data();
+  o.init = init.data();
+  o.n_grad = ngrad.data();
+  o.seconds = secs.data();
+  int r = gbnuts_sample_run(m, &rc, &o, cb);
+  if (r == GBNUTS_CONFIG) {
+    emit_log(cb, GBNUTS_ERROR, last_error());
+    return r;
+  }
+  if (r) return r;
+  // set-up failures are reported before any chain runs (hmc_nuts_diag_e_adapt.hpp:359-385)
+  for (int c = 0; c < C; ++c) {
+    if (status[c] == GBNUTS_CHAIN_INIT_FAILED) {
+      if (rc.init_radius != 0.0 && !rc.inits) {
+        emit_log(cb, GBNUTS_INFO, "");
+        emit_log(cb, GBNUTS_ERROR, "Initialization between (-" + fmt(rc.init_radius) + ", " +
+                                       fmt(rc.init_radius) + ") failed after 100 attempts. ");
+        emit_log(cb, GBNUTS_ERROR,
+                 " Try specifying initial values, reducing ranges of constrained values, "
+                 "or reparameterizing the model.");
+      }
+      emit_log(cb, GBNUTS_ERROR, "Initialization failed.");
+      return GBNUTS_CONFIG;
+    }
+  }
+  std::vector<std::string> cnames, unames;
+  host_names(m->desc, true, cnames);
+  host_names(m->desc, false, unames);
+  std::vector<std::string> sample_names = {"lp__", "accept_stat__", "stepsize__", "treedepth__",
+                                           "n_leapfrog__", "divergent__", "energy__"};
+  std::vector<std::string> snames = sample_names;
+  snames.insert(snames.end(), cnames.begin(), cnames.end());
+  std::vector<std::string> dnames = sample_names;
+  for (auto& s : unames) dnames.push_back(s);
+  for (auto& s : unames) dnames.push_back("p_" + s);
+  for (auto& s : unames) dnames.push_back("g_" + s);
+  int code = GBNUTS_OK;
+  std::vector<double> drow(7 + 3 * D);
+  for (int c = 0; c < C; ++c) {
+    emit_values(cb, c, GBNUTS_INIT_WRITER, init.data() + (size_t)c * D, D);
+    if (status[c] == GBNUTS_CHAIN_STEPSIZE_INIT_FAILED) {
+      // run_adaptive_sampler.hpp:61-68
+      emit_log(cb, GBNUTS_ERROR, "Exception initializing step size.");
+      emit_log(cb, GBNUTS_ERROR, "Posterior is improper. Please check your model.");
+      continue;
+    }
+    emit_names(cb, c, GBNUTS_SAMPLE_WRITER, snames);
+    emit_names(cb, c, GBNUTS_DIAGNOSTIC_WRITER, dnames);
+    const double* base = draws.data() + (size_t)c * o.max_rows * n_cols;
+    auto write_rows = [&](int from, int to) {
+      for (int i = from; i < to; ++i) {
+        emit_values(cb, c, GBNUTS_SAMPLE_WRITER, base + (size_t)i * n_cols, n_cols);
+        if (diag) {
+          memcpy(drow.data(), base + (size_t)i * n_cols, 7 * sizeof(double));
+          memcpy(drow.data() + 7, dg.data() + ((size_t)c * o.max_rows + i) * 3 * D,
+                 3 * D * sizeof(double));
+          emit_values(cb, c, GBNUTS_DIAGNOSTIC_WRITER, drow.data(), 7 + 3 * D);
+        }
+      }
+    };
+    write_rows(0, n_warm[c]);
+    const bool complete = status[c] == GBNUTS_CHAIN_OK;
+    if (complete || n_rows[c] > n_warm[c]) {
+      // mcmc_writer::write_adapt_finish + base_hmc::write_sampler_state
+      emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Adaptation terminated");
+      emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Step size = " + fmt(eps[c]));
+      emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Diagonal elements of inverse mass matrix:");
+      std::ostringstream s;
+      for (int d = 0; d < D; ++d) s << (d ? ", " : "") << invm[(size_t)c * D + d];
+      emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, s.str());
+      if (rc.adapt && cb && cb->write_metric)
+        cb->write_metric(cb->ctx, c, eps[c], "diag_e", invm.data() + (size_t)c * D, D);
+    }
+    write_rows(n_warm[c], n_rows[c]);
+    if (status[c] == GBNUTS_CHAIN_OK) {
+      write_timing(cb, c, GBNUTS_SAMPLE_WRITER, secs[2 * c], secs[2 * c + 1]);
+      write_timing(cb, c, GBNUTS_DIAGNOSTIC_WRITER, secs[2 * c], secs[2 * c + 1]);
+      const std::string title(" Elapsed Time: ");
+      emit_log(cb, GBNUTS_INFO, "");
+      emit_log(cb, GBNUTS_INFO, title + fmt(secs[2 * c]) + " seconds (Warm-up)");
+      emit_log(cb, GBNUTS_INFO,
+               std::string(title.size(), ' ') + fmt(secs[2 * c + 1]) + " seconds (Sampling)");
+      emit_log(cb, GBNUTS_INFO, std::string(title.size(), ' ') +
+                                    fmt(secs[2 * c] + secs[2 * c + 1]) + " seconds (Total)");
+      emit_log(cb, GBNUTS_INFO, "");
+    } else if (status[c] == GBNUTS_CHAIN_STEPSIZE_FAILED ||
+               status[c] == GBNUTS_CHAIN_METRIC_OVERFLOW ||
+               status[c] == GBNUTS_CHAIN_INTERRUPTED) {
+      if (status[c] == GBNUTS_CHAIN_METRIC_OVERFLOW)
+        emit_log(cb, GBNUTS_ERROR,
+                 "Numerical overflow in metric adaptation. This occurs when the sampler "
+                 "encounters extreme values on the unconstrained space; this may happen when "
+                 "the posterior density function is too wide or improper. There may be "
+                 "problems with your model specification.");
+      else if (status[c] == GBNUTS_CHAIN_STEPSIZE_FAILED)
+        emit_log(cb, GBNUTS_ERROR, "Posterior is improper. Please check your model.");
+      else
+        emit_log(cb, GBNUTS_ERROR, "Sampling interrupted.");
+      code = GBNUTS_SOFTWARE;
+    }
+  }
+  return code;
+}
+
+}  // namespace
+
+extern "C" int gbnuts_hmc_nuts_diag_e_adapt(
+    gbnuts_model* m, int num_chains, const double* inits, const double* inv_metrics,
+    unsigned random_seed, unsigned init_chain_id, double init_radius, int num_warmup,
+    int num_samples, int num_thin, int save_warmup, int refresh, double stepsize,
+    double stepsize_jitter, int max_depth, double delta, double gamma, double kappa, double t0,
+    unsigned init_buffer, unsigned term_buffer, unsigned window, int precision,
+    const gbnuts_callbacks* cb) {
+  (void)refresh;
+  gbnuts_run_config rc;
+  memset(&rc, 0, sizeof(rc));
+  rc.num_chains = num_chains;
+  rc.adapt = 1;
+  rc.num_warmup = num_warmup;
+  rc.num_samples = num_samples;
+  rc.num_thin = num_thin;
+  rc.save_warmup = save_warmup;
+  rc.stepsize = stepsize;
+  rc.stepsize_jitter = stepsize_jitter;
+  rc.max_depth = max_depth;
+  rc.delta = delta;
+  rc.gamma = gamma;
+  rc.kappa = kappa;
+  rc.t0 = t0;
+  rc.init_buffer = init_buffer;
+  rc.term_buffer = term_buffer;
+  rc.window = window;
+  rc.init_radius = init_radius;
+  rc.random_seed = random_seed;
+  rc.init_chain_id = init_chain_id;
+  rc.precision = precision;
+  rc.inits = inits;
+  rc.inv_metrics = inv_metrics;
+  return run_service(m, rc, cb);
+}
+
+extern "C" int gbnuts_hmc_nuts_diag_e(gbnuts_model* m, int num_chains, const double* inits,
+                                      const double* inv_metrics, unsigned random_seed,
+                                      unsigned init_chain_id, double init_radius,
+                                      int num_warmup, int num_samples, int num_thin,
+                                      int save_warmup, int refresh, double stepsize,
+                                      double stepsize_jitter, int max_depth, int precision,
+                                      const gbnuts_callbacks* cb) {
+  (void)refresh;
+  gbnuts_run_config rc;
+  memset(&rc, 0, sizeof(rc));
+  rc.num_chains = num_chains;
+  rc.adapt = 0;
+  rc.num_warmup = num_warmup;
+  rc.num_samples = num_samples;
+  rc.num_thin = num_thin;
+  rc.save_warmup = save_warmup;
+  rc.stepsize = stepsize;
+  rc.stepsize_jitter = stepsize_jitter;
+  rc.max_depth = max_depth;
+  rc.init_radius = init_radius;
+  rc.random_seed = random_seed;
+  rc.init_chain_id = init_chain_id;
+  rc.precision = precision;
+  rc.inits = inits;
+  rc.inv_metrics = inv_metrics;
+  return run_service(m, rc, cb);
+}

@@ -1,0 +1,79 @@
+// Internal interfaces shared by the gbnuts translation units (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#define GBN_CUDA_TRY(expr)                                                       \
+  do {                                                                           \
+    cudaError_t _e = (expr);                                                     \
+    if (_e != cudaSuccess) {                                                     \
+      gbn::set_last_error(std::string(#expr) + ": " + cudaGetErrorString(_e));  \
+      return GBNUTS_SOFTWARE;                                                    \
+    }                                                                            \
+  } while (0)
+
+namespace gbn {
+
+void set_last_error(const std::string& s);
+const std::string& last_error();
+
+enum Link { LINK_LOGIT = 0, LINK_POISSON_LOG = 1, LINK_NORMAL = 2 };
+
+// A log density on the device.  theta layout per family:
+//   LOGISTIC / POISSON : [alpha], beta[K]
+//   HIER_NORMAL        : mu, log tau, log sigma, z[J], beta[K]
+//   HIER_LOGISTIC      : alpha, log tau, z[J], beta[K]
+// Every family is  eta_n = base + tau z_{g(n)} + x_n . beta  with a link.
+struct ModelDesc {
+  int kind;
+  int link;
+  long long N;
+  int K, J, D;
+  int has_base;   // theta[0] enters eta with coefficient 1
+  int idx_tau;    // index of log tau in theta, or -1
+  int idx_sigma;  // index of log sigma in theta, or -1
+  int off_z;      // first z index, or -1
+  int off_beta;   // first beta index
+  int x_dtype;    // GBNUTS_F64 / F32 / BF16
+  const void* X;  // N x K row-major
+  const double* y;
+  const int* group;  // N (hierarchical) or nullptr
+  double s_base, s_tau, s_sigma, s_beta;  // prior scales
+  double sum_lgamma_y;                    // Poisson constant, for propto = false
+};
+
+// Number of per-(split, chain) partial sums: lp, sum r, sum r z_g, sum e^2, beta[K].
+inline int n_partials(const ModelDesc& m) { return 4 + m.K; }
+
+// Workspace for one batched gradient evaluation of C chains.
+struct GradWorkspace {
+  int C = 0, S = 0, NP = 0;
+  double* partial = nullptr;   // [S][C][NP]
+  double* gz = nullptr;        // [C][J] raw group sums (hierarchical)
+  long long* split_rows = nullptr;  // [S+1] device
+  std::vector<long long> h_split_rows;
+  size_t bytes = 0;
+};
+
+// Chooses the split count and sets split row boundaries (group aligned for
+// hierarchical models).  Allocates (or reuses) the workspace.
+int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int precision,
+                      GradWorkspace& ws);
+void free_workspace(GradWorkspace& ws);
+
+// lp[C] and grad[C][ldg] of C chains at Q[C][ldq] (device pointers), with
+// Stan's propto/jacobian semantics; active (may be null) masks chains.
+int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int ldq,
+                         int C, const int* active, double* lp, double* grad, int ldg,
+                         int propto, int jacobian, GradWorkspace& ws,
+                         cudaStream_t stream, cudaEvent_t ev0, cudaEvent_t ev1);
+
+// Maximum chains per block of the partial kernel for a given K (0 if K is
+// beyond what the kernel supports).
+int chains_per_block(int K);
+
+}  // namespace gbn

@@ -1,0 +1,492 @@
+// Batched log density and gradient for C chains (the sampler's
+// update_potential_gradient, src/stan/mcmc/hmc/hamiltonians/base_hamiltonian.hpp:61-70,
+// for every chain at once).
+//
+// Every supported family has the form
+//     eta_n = base + tau * z[g(n)] + x_n . beta,     lp = sum_n link(eta_n, y_n) + priors
+// so one kernel covers all of them:
+//   * loglik_partial_kernel: grid (row split s, chain block).  A CTA stages a
+//     tile of X rows in shared memory (converted to the compute type), computes
+//     eta for CB chains, applies the link (lp term, residual r = dlp/deta),
+//     then accumulates X^T r for its chains over all tiles of its row range.
+//     Group sums (sum of r over the rows of each group, for d/dz) come from a
+//     warp segmented scan over the group-sorted rows, carried across tiles;
+//     split boundaries are group aligned so each group sum has one writer.
+//   * loglik_finalize_kernel: per chain, sums the split partials in split
+//     order (deterministic) and adds priors, Jacobians and the chain rule
+//     through tau = exp(u), sigma = exp(u).
+// FP64 form: every operation in double.  FP32 form: X.beta, link and X^T r
+// in single precision inside a split, partial and final sums in double.
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "../../include/gbnuts.h"
+#include "gbnuts_internal.h"
+
+namespace gbn {
+
+static constexpr int kThreads = 256;
+static constexpr int kMaxPairs = 32;  // (chain, feature) adjoint pairs per thread
+
+int chains_per_block(int K) {
+  if (K <= 512) return 16;
+  if (K <= 1024) return 8;
+  if (K <= 2048) return 4;
+  return 0;
+}
+
+template <typename XT>
+__device__ __forceinline__ double x_to_double(XT v);
+template <>
+__device__ __forceinline__ double x_to_double<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ double x_to_double<float>(float v) { return (double)v; }
+template <>
+__device__ __forceinline__ double x_to_double<uint16_t>(uint16_t v) {
+  return (double)__uint_as_float(((unsigned)v) << 16);
+}
+
+template <typename CT>
+__device__ __forceinline__ void apply_link(int link, CT eta, CT y, CT inv_s2, CT& term,
+                                           CT& resid, CT& sq) {
+  if (link == LINK_LOGIT) {
+    CT e = exp(-fabs(eta));
+    CT sp = (eta > CT(0) ? eta : CT(0)) + log1p(e);
+    term = y * eta - sp;
+    CT sig = eta >= CT(0) ? CT(1) / (CT(1) + e) : e / (CT(1) + e);
+    resid = y - sig;
+    sq = CT(0);
+  } else if (link == LINK_POISSON_LOG) {
+    CT mu = exp(eta);
+    term = y * eta - mu;
+    resid = y - mu;
+    sq = CT(0);
+  } else {
+    CT e = y - eta;
+    term = CT(-0.5) * e * e * inv_s2;
+    resid = e * inv_s2;
+    sq = e * e;
+  }
+}
+
+// Shared memory of the partial kernel, in elements of the compute type.
+template <typename CT>
+__host__ __device__ inline size_t partial_smem_bytes(int CB, int K, int RB) {
+  const int KP = K + 1;
+  return sizeof(CT) * ((size_t)CB * KP + (size_t)RB * KP + (size_t)RB * CB + RB) +
+         sizeof(int) * (size_t)RB;
+}
+
+template <typename XT, typename CT, int CB>
+__global__ void __launch_bounds__(kThreads)
+    loglik_partial_kernel(ModelDesc m, const double* __restrict__ Q, int ldq, int C,
+                          const int* __restrict__ active,
+                          const long long* __restrict__ split_rows, int RB,
+                          double* __restrict__ P, int NP, double* __restrict__ Gz) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int K = m.K;
+  const int KP = K + 1;
+  CT* th_s = reinterpret_cast<CT*>(smem_raw);  // [CB][KP]
+  CT* x_s = th_s + (size_t)CB * KP;            // [RB][KP]
+  CT* r_s = x_s + (size_t)RB * KP;             // [RB][CB]
+  CT* y_s = r_s + (size_t)RB * CB;             // [RB]
+  int* g_s = reinterpret_cast<int*>(y_s + RB);  // [RB]
+  __shared__ CT base_s[CB], tau_s[CB], invs2_s[CB];
+  __shared__ int act_s[CB];
+  __shared__ double red_s[kThreads][4];
+
+  const int tid = threadIdx.x;
+  const int s = blockIdx.x;
+  const int c0 = blockIdx.y * CB;
+  const XT* __restrict__ X = static_cast<const XT*>(m.X);
+
+  for (int idx = tid; idx < CB * K; idx += kThreads) {
+    int c = idx / K, k = idx - c * K;
+    int cg = c0 + c;
+    th_s[c * KP + k] = (cg < C) ? (CT)Q[(size_t)cg * ldq + m.off_beta + k] : CT(0);
+  }
+  if (tid < CB) {
+    int cg = c0 + tid;
+    int act = (cg < C) && (active == nullptr || active[cg] != 0);
+    act_s[tid] = act;
+    const double* th = Q + (size_t)(act ? cg : 0) * ldq;
+    base_s[tid] = (act && m.has_base) ? (CT)th[0] : CT(0);
+    tau_s[tid] = (act && m.idx_tau >= 0) ? (CT)exp(th[m.idx_tau]) : CT(0);
+    double sig = (act && m.idx_sigma >= 0) ? exp(th[m.idx_sigma]) : 1.0;
+    invs2_s[tid] = (CT)(1.0 / (sig * sig));
+  }
+  int any = (tid < CB) ? act_s[tid] : 0;
+  if (!__syncthreads_or(any)) return;
+
+  const long long row_begin = split_rows[s], row_end = split_rows[s + 1];
+  constexpr int RPT = kThreads / CB;  // row lanes per pass
+  const int my_c = tid % CB, my_rl = tid / CB;
+  const int warp = tid >> 5, lane = tid & 31;
+  const bool has_z = m.off_z >= 0;
+  double lp_d = 0, base_d = 0, tau_d = 0, sq_d = 0;
+  CT acc[kMaxPairs];
+#pragma unroll
+  for (int j = 0; j < kMaxPairs; ++j) acc[j] = CT(0);
+  // segmented-scan carry for the group sums, per (warp, chain slot)
+  constexpr int kChainsPerWarp = (CB + 7) / 8;
+  int carry_key[kChainsPerWarp];
+  CT carry_val[kChainsPerWarp];
+#pragma unroll
+  for (int i = 0; i < kChainsPerWarp; ++i) {
+    carry_key[i] = -1;
+    carry_val[i] = CT(0);
+  }
+
+  for (long long r0 = row_begin; r0 < row_end; r0 += RB) {
+    const int nrows = (int)min((long long)RB, row_end - r0);
+    __syncthreads();
+    const XT* xt = X + (size_t)r0 * K;
+    for (int idx = tid; idx < nrows * K; idx += kThreads) {
+      int r = idx / K, k = idx - r * K;
+      x_s[r * KP + k] = (CT)x_to_double<XT>(xt[idx]);
+    }
+    for (int idx = tid; idx < RB; idx += kThreads) {
+      y_s[idx] = idx < nrows ? (CT)m.y[r0 + idx] : CT(0);
+      g_s[idx] = (has_z && idx < nrows) ? m.group[r0 + idx] : -1;
+    }
+    __syncthreads();
+
+    // forward: eta, link, per-chain scalar sums
+    {
+      CT lp_t = 0, base_t = 0, tau_t = 0, sq_t = 0;
+      const bool cact = act_s[my_c] != 0;
+      const CT* tc = th_s + my_c * KP;
+      const double* thq = Q + (size_t)(c0 + my_c) * ldq;
+      for (int r = my_rl; r < RB; r += RPT) {
+        CT resid = CT(0);
+        if (cact && r < nrows) {
+          const CT* xr = x_s + r * KP;
+          CT dotv = CT(0);
+          for (int k = 0; k < K; ++k) dotv = fma(xr[k], tc[k], dotv);
+          CT eta = base_s[my_c] + dotv;
+          CT zg = CT(0);
+          if (has_z) {
+            zg = (CT)thq[m.off_z + g_s[r]];
+            eta += tau_s[my_c] * zg;
+          }
+          CT term, sq;
+          apply_link<CT>(m.link, eta, y_s[r], invs2_s[my_c], term, resid, sq);
+          lp_t += term;
+          base_t += resid;
+          tau_t += resid * zg;
+          sq_t += sq;
+        }
+        r_s[r * CB + my_c] = resid;
+      }
+      lp_d += (double)lp_t;
+      base_d += (double)base_t;
+      tau_d += (double)tau_t;
+      sq_d += (double)sq_t;
+    }
+    __syncthreads();
+
+    // adjoint: X^T r for (chain, feature) pairs
+#pragma unroll
+    for (int j = 0; j < kMaxPairs; ++j) {
+      int p = tid + kThreads * j;
+      if (p < CB * K) {
+        int c = p / K, k = p - c * K;
+        CT a = CT(0);
+        for (int r = 0; r < nrows; ++r) a = fma(x_s[r * KP + k], r_s[r * CB + c], a);
+        acc[j] += a;
+      }
+    }
+
+    // group sums: warp w handles chain slots w, w + 8, ...
+    if (has_z) {
+#pragma unroll
+      for (int i = 0; i < kChainsPerWarp; ++i) {
+        const int c = warp + 8 * i;
+        if (c < CB && act_s[c]) {
+          const int cg = c0 + c;
+          for (int rb = 0; rb < nrows; rb += 32) {
+            const int r = rb + lane;
+            int key = r < nrows ? g_s[r] : -2 - lane;
+            CT val = r < nrows ? r_s[r * CB + c] : CT(0);
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+              CT v = __shfl_up_sync(0xffffffffu, val, off);
+              int kk = __shfl_up_sync(0xffffffffu, key, off);
+              if (lane >= off && kk == key) val += v;
+            }
+            int next_key = __shfl_down_sync(0xffffffffu, key, 1);
+            bool seg_end = (lane == 31) || (next_key != key);
+            // the first segment of the chunk continues the carried one
+            int first_key = __shfl_sync(0xffffffffu, key, 0);
+            if (key == first_key && key == carry_key[i]) val += carry_val[i];
+            int last_key = __shfl_sync(0xffffffffu, key, 31);
+            CT last_val = __shfl_sync(0xffffffffu, val, 31);
+            if (seg_end && r < nrows && lane != 31) Gz[(size_t)cg * m.J + key] = (double)val;
+            // the chunk's last segment may continue into the next chunk
+            if (last_key >= 0) {
+              if (carry_key[i] >= 0 && carry_key[i] != first_key && lane == 0) {
+                // carried segment ended exactly at the previous chunk boundary
+                Gz[(size_t)cg * m.J + carry_key[i]] = (double)carry_val[i];
+              }
+              carry_key[i] = last_key;
+              carry_val[i] = last_val;
+            } else {
+              // partial chunk ending the tile: last valid lane closes its segment
+              // (it was written above unless it is lane 31, impossible here)
+              if (carry_key[i] >= 0 && carry_key[i] != first_key && lane == 0)
+                Gz[(size_t)cg * m.J + carry_key[i]] = (double)carry_val[i];
+              carry_key[i] = -1;
+              carry_val[i] = CT(0);
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // flush open group segments
+  if (has_z && lane == 0) {
+#pragma unroll
+    for (int i = 0; i < kChainsPerWarp; ++i) {
+      const int c = warp + 8 * i;
+      if (c < CB && act_s[c] && carry_key[i] >= 0)
+        Gz[(size_t)(c0 + c) * m.J + carry_key[i]] = (double)carry_val[i];
+    }
+  }
+
+#pragma unroll
+  for (int j = 0; j < kMaxPairs; ++j) {
+    int p = tid + kThreads * j;
+    if (p < CB * K) {
+      int c = p / K, k = p - c * K;
+      if (act_s[c]) P[((size_t)s * C + c0 + c) * NP + 4 + k] = (double)acc[j];
+    }
+  }
+  red_s[tid][0] = lp_d;
+  red_s[tid][1] = base_d;
+  red_s[tid][2] = tau_d;
+  red_s[tid][3] = sq_d;
+  __syncthreads();
+  if (tid < CB && act_s[tid]) {
+    double v[4] = {0, 0, 0, 0};
+    for (int rl = 0; rl < RPT; ++rl)
+      for (int q = 0; q < 4; ++q) v[q] += red_s[rl * CB + tid][q];
+    double* dst = P + ((size_t)s * C + c0 + tid) * NP;
+    for (int q = 0; q < 4; ++q) dst[q] = v[q];
+  }
+}
+
+static constexpr double kLogSqrt2Pi = 0.91893853320467274178032973640562;
+
+// Per chain: split sums + priors + Jacobians -> lp, grad.
+__global__ void __launch_bounds__(128)
+    loglik_finalize_kernel(ModelDesc m, const double* __restrict__ Q, int ldq, int C,
+                           const int* __restrict__ active, const double* __restrict__ P,
+                           int NP, int S, const double* __restrict__ Gz,
+                           double* __restrict__ lp_out, double* __restrict__ grad, int ldg,
+                           int propto, int jacobian) {
+  const int c = blockIdx.x;
+  if (c >= C) return;
+  if (active && !active[c]) return;
+  const int tid = threadIdx.x;
+  const double* th = Q + (size_t)c * ldq;
+  const double tau = m.idx_tau >= 0 ? exp(th[m.idx_tau]) : 0.0;
+  const double jac = jacobian ? 1.0 : 0.0;
+  double prior = 0.0;
+  for (int d = tid; d < m.D; d += blockDim.x) {
+    const double t = th[d];
+    double g;
+    if (d >= m.off_beta) {
+      const int k = d - m.off_beta;
+      double sum = 0;
+      for (int s = 0; s < S; ++s) sum += P[((size_t)s * C + c) * NP + 4 + k];
+      g = sum - t / (m.s_beta * m.s_beta);
+      double z = t / m.s_beta;
+      prior += -0.5 * z * z;
+      if (!propto) prior += -log(m.s_beta) - kLogSqrt2Pi;
+    } else if (d == 0 && m.has_base) {
+      double sum = 0;
+      for (int s = 0; s < S; ++s) sum += P[((size_t)s * C + c) * NP + 1];
+      g = sum - t / (m.s_base * m.s_base);
+      double z = t / m.s_base;
+      prior += -0.5 * z * z;
+      if (!propto) prior += -log(m.s_base) - kLogSqrt2Pi;
+    } else if (d == m.idx_tau) {
+      double sum = 0;
+      for (int s = 0; s < S; ++s) sum += P[((size_t)s * C + c) * NP + 2];
+      g = tau * (sum - tau / (m.s_tau * m.s_tau)) + jac;
+      double z = tau / m.s_tau;
+      prior += -0.5 * z * z + jac * t;
+      if (!propto) prior += -log(m.s_tau) - kLogSqrt2Pi;
+    } else if (d == m.idx_sigma) {
+      const double sigma = exp(t);
+      double sum = 0;
+      for (int s = 0; s < S; ++s) sum += P[((size_t)s * C + c) * NP + 3];
+      const double dsig = -(double)m.N / sigma + sum / (sigma * sigma * sigma) -
+                          sigma / (m.s_sigma * m.s_sigma);
+      g = sigma * dsig + jac;
+      double z = sigma / m.s_sigma;
+      prior += -0.5 * z * z + jac * t - (double)m.N * t;
+      if (!propto) prior += -log(m.s_sigma) - kLogSqrt2Pi;
+    } else {  // z_j
+      const int j = d - m.off_z;
+      g = tau * Gz[(size_t)c * m.J + j] - t;
+      prior += -0.5 * t * t;
+      if (!propto) prior += -kLogSqrt2Pi;
+    }
+    grad[(size_t)c * ldg + d] = g;
+  }
+  __shared__ double red[128];
+  red[tid] = prior;
+  __syncthreads();
+  for (int w = 64; w > 0; w >>= 1) {
+    if (tid < w) red[tid] += red[tid + w];
+    __syncthreads();
+  }
+  if (tid == 0) {
+    double sum = 0;
+    for (int s = 0; s < S; ++s) sum += P[((size_t)s * C + c) * NP + 0];
+    double lp = sum + red[0];
+    if (!propto) {
+      if (m.link == LINK_NORMAL) lp += -(double)m.N * kLogSqrt2Pi;
+      if (m.link == LINK_POISSON_LOG) lp += -m.sum_lgamma_y;
+    }
+    lp_out[c] = lp;
+  }
+}
+
+// ------------------------------------------------------------------ host side
+static std::mutex g_attr_mu;
+
+template <typename XT, typename CT, int CB>
+static void set_smem_attr(size_t bytes) {
+  static size_t done = 0;
+  std::lock_guard<std::mutex> lk(g_attr_mu);
+  if (bytes > done) {
+    cudaFuncSetAttribute(loglik_partial_kernel<XT, CT, CB>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    done = bytes;
+  }
+}
+
+static constexpr size_t kSmemBudget = 150 * 1024;
+
+template <typename CT>
+static int choose_rb(int CB, int K) {
+  int rb = 256;
+  while (rb > 32 && partial_smem_bytes<CT>(CB, K, rb) > kSmemBudget) rb -= 32;
+  return rb;
+}
+
+template <typename XT, typename CT, int CB>
+static void launch_partial(const ModelDesc& m, const double* Q, int ldq, int C,
+                           const int* active, GradWorkspace& ws, cudaStream_t st) {
+  const int RB = choose_rb<CT>(CB, m.K);
+  const size_t smem = partial_smem_bytes<CT>(CB, m.K, RB);
+  set_smem_attr<XT, CT, CB>(smem);
+  dim3 grid(ws.S, (C + CB - 1) / CB);
+  loglik_partial_kernel<XT, CT, CB><<<grid, kThreads, smem, st>>>(
+      m, Q, ldq, C, active, ws.split_rows, RB, ws.partial, ws.NP, ws.gz);
+}
+
+template <typename XT, typename CT>
+static void dispatch_cb(const ModelDesc& m, const double* Q, int ldq, int C,
+                        const int* active, GradWorkspace& ws, cudaStream_t st) {
+  switch (chains_per_block(m.K)) {
+    case 16: launch_partial<XT, CT, 16>(m, Q, ldq, C, active, ws, st); break;
+    case 8: launch_partial<XT, CT, 8>(m, Q, ldq, C, active, ws, st); break;
+    default: launch_partial<XT, CT, 4>(m, Q, ldq, C, active, ws, st); break;
+  }
+}
+
+template <typename CT>
+static void dispatch_x(const ModelDesc& m, const double* Q, int ldq, int C,
+                       const int* active, GradWorkspace& ws, cudaStream_t st) {
+  if (m.x_dtype == GBNUTS_F64)
+    dispatch_cb<double, CT>(m, Q, ldq, C, active, ws, st);
+  else if (m.x_dtype == GBNUTS_F32)
+    dispatch_cb<float, CT>(m, Q, ldq, C, active, ws, st);
+  else
+    dispatch_cb<uint16_t, CT>(m, Q, ldq, C, active, ws, st);
+}
+
+int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int precision,
+                      GradWorkspace& ws) {
+  (void)precision;
+  const int CB = chains_per_block(m.K);
+  if (CB == 0) {
+    set_last_error("K beyond the supported maximum (2048)");
+    return GBNUTS_USAGE;
+  }
+  const int chain_blocks = (C + CB - 1) / CB;
+  // Splits: enough CTAs for ~2 waves over 152 SMs, at least 64 rows each.
+  long long max_s = std::max(1LL, m.N / 64);
+  int S = (int)std::min<long long>(max_s, std::max(1, (2 * 152 + chain_blocks - 1) / chain_blocks));
+  if (m.off_z >= 0) S = std::min(S, m.J);
+  S = std::max(S, 1);
+  const int NP = n_partials(m);
+  size_t need = (size_t)S * C * NP * sizeof(double) +
+                (m.off_z >= 0 ? (size_t)C * m.J * sizeof(double) : 0) +
+                (size_t)(S + 1) * sizeof(long long);
+  if (ws.C == C && ws.S == S && ws.NP == NP && ws.partial) return GBNUTS_OK;
+  free_workspace(ws);
+  ws.C = C;
+  ws.S = S;
+  ws.NP = NP;
+  ws.h_split_rows.assign(S + 1, 0);
+  for (int s = 0; s <= S; ++s) {
+    if (m.off_z >= 0) {
+      long long j = (long long)m.J * s / S;
+      ws.h_split_rows[s] = h_group_off[j];
+    } else {
+      ws.h_split_rows[s] = m.N * s / S;
+    }
+  }
+  char* base = nullptr;
+  GBN_CUDA_TRY(cudaMalloc(&base, need));
+  ws.bytes = need;
+  ws.partial = reinterpret_cast<double*>(base);
+  size_t off = (size_t)S * C * NP * sizeof(double);
+  if (m.off_z >= 0) {
+    ws.gz = reinterpret_cast<double*>(base + off);
+    off += (size_t)C * m.J * sizeof(double);
+  }
+  ws.split_rows = reinterpret_cast<long long*>(base + off);
+  GBN_CUDA_TRY(cudaMemcpy(ws.split_rows, ws.h_split_rows.data(),
+                          (S + 1) * sizeof(long long), cudaMemcpyHostToDevice));
+  return GBNUTS_OK;
+}
+
+void free_workspace(GradWorkspace& ws) {
+  if (ws.partial) cudaFree(ws.partial);
+  ws = GradWorkspace();
+}
+
+int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int ldq,
+                         int C, const int* active, double* lp, double* grad, int ldg,
+                         int propto, int jacobian, GradWorkspace& ws,
+                         cudaStream_t stream, cudaEvent_t ev0, cudaEvent_t ev1) {
+  if (m.off_z >= 0)
+    GBN_CUDA_TRY(cudaMemsetAsync(ws.gz, 0, (size_t)C * m.J * sizeof(double), stream));
+  if (ev0) cudaEventRecord(ev0, stream);
+  if (precision == GBNUTS_PREC_FP64) {
+    dispatch_x<double>(m, Q, ldq, C, active, ws, stream);
+  } else if (precision == GBNUTS_PREC_FP32) {
+    dispatch_x<float>(m, Q, ldq, C, active, ws, stream);
+  } else {
+    set_last_error("precision not available for this model");
+    return GBNUTS_USAGE;
+  }
+  GBN_CUDA_TRY(cudaGetLastError());
+  if (ev1) cudaEventRecord(ev1, stream);
+  loglik_finalize_kernel<<<C, 128, 0, stream>>>(m, Q, ldq, C, active, ws.partial, ws.NP,
+                                                ws.S, ws.gz, lp, grad, ldg, propto,
+                                                jacobian);
+  GBN_CUDA_TRY(cudaGetLastError());
+  return GBNUTS_OK;
+}
+
+}  // namespace gbn

@@ -1,0 +1,840 @@
+// Device NUTS (diag_e metric, multinomial sampling, adaptation) for many
+// chains: one warp per chain, a state machine that runs until the chain needs
+// its next gradient, writes the position it needs it at, and yields.  A
+// batched gradient over all chains that yielded follows; the next launch
+// resumes every chain with its gradient.  Chains never wait for one another,
+// so a chain that finishes a short trajectory starts its next transition at
+// once (its next gradient shares the batch with other chains' deep trees).
+//
+// Restated from (paths relative to the stan-dev/stan tree):
+//   base_nuts::transition / build_tree   src/stan/mcmc/hmc/nuts/base_nuts.hpp:78-352
+//   adapt_diag_e_nuts::transition        src/stan/mcmc/hmc/nuts/adapt_diag_e_nuts.hpp:25-48
+//   base_hmc::init_stepsize, sample_stepsize  src/stan/mcmc/hmc/base_hmc.hpp:93-200
+//   diag_e_metric (T, dtau_dp, sample_p) src/stan/mcmc/hmc/hamiltonians/diag_e_metric.hpp:20-50
+//   expl_leapfrog                        src/stan/mcmc/hmc/integrators/expl_leapfrog.hpp:16-32
+//   stepsize_adaptation                  src/stan/mcmc/stepsize_adaptation.hpp:55-73
+//   windowed_adaptation, var_adaptation  src/stan/mcmc/windowed_adaptation.hpp:29-110,
+//                                        src/stan/mcmc/var_adaptation.hpp:17-46
+//   initialize (random inits, retries)   src/stan/services/util/initialize.hpp:68-227
+//   generate_transitions (thinning)      src/stan/services/util/generate_transitions.hpp:51-76
+//
+// The recursion of build_tree becomes iteration over the 2^d leaves of a new
+// subtree: after leaf i, the subtrees completed by that leaf are merged bottom
+// up (one merge per trailing one bit of i), each merge doing exactly the
+// reference's proposal draw, log-sum-exp and three U-turn checks.  An
+// unfinished left sibling of depth l waits in stack level l (proposal point,
+// momenta at both ends, summed momentum rho, log sum weight).  Uniform draws
+// are therefore consumed in the reference's order.  Elementwise updates use
+// explicit round-to-nearest operations so they round exactly like the host
+// oracle compiled without contraction.
+#include <math.h>
+
+#include "../../include/gbnuts.h"
+#include "../../include/gbnuts_draw_stream.h"
+#include "nuts_device.h"
+
+namespace gbn {
+
+#define DMUL(a, b) __dmul_rn((a), (b))
+#define DADD(a, b) __dadd_rn((a), (b))
+#define DSUB(a, b) __dsub_rn((a), (b))
+#define DDIV(a, b) __ddiv_rn((a), (b))
+
+static __device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+static __device__ __forceinline__ double log1p_exp_d(double a) {
+  if (a > 0.0) return a + log1p(exp(-a));
+  return log1p(exp(a));
+}
+
+// stan::math::log_sum_exp (called at base_nuts.hpp:172,265,323-324)
+static __device__ __forceinline__ double log_sum_exp_d(double a, double b) {
+  const double inf = __longlong_as_double(0x7ff0000000000000LL);
+  if (a == -inf) return b;
+  if (a == inf && b == inf) return inf;
+  if (a > b) return a + log1p_exp_d(b - a);
+  return b + log1p_exp_d(a - b);
+}
+
+struct Ctx {
+  const SamplerCfg& cfg;
+  double* vecs;
+  int c, lane;
+  __device__ double* slot(int s) const {
+    return vecs + ((size_t)c * cfg.n_slots + s) * cfg.ld;
+  }
+};
+
+// T(p) = 1/2 p . (invM p)  (diag_e_metric.hpp:20-22)
+static __device__ double kinetic(const Ctx& x, const double* p) {
+  const double* im = x.slot(SL_INVM);
+  double s = 0.0;
+  for (int i = x.lane; i < x.cfg.D; i += 32) s += p[i] * DMUL(im[i], p[i]);
+  return 0.5 * warp_sum(s);
+}
+
+static __device__ __forceinline__ double draw_uniform(const SamplerCfg& cfg, ChainState& st,
+                                                      int c) {
+  return gbds_uniform_at(cfg.seed, cfg.init_chain_id + (unsigned)c, st.nu++);
+}
+
+// sample_p (diag_e_metric.hpp:44-50): p_i = n_i / sqrt(invM_i), D normals.
+static __device__ void sample_p(const Ctx& x, ChainState& st, double* p) {
+  const double* im = x.slot(SL_INVM);
+  const unsigned chain = x.cfg.init_chain_id + (unsigned)x.c;
+  for (int i = x.lane; i < x.cfg.D; i += 32)
+    p[i] = DDIV(gbds_normal_at(x.cfg.seed, chain, st.nn + i), __dsqrt_rn(im[i]));
+  st.nn += x.cfg.D;
+}
+
+static __device__ void copy_vec(const Ctx& x, double* dst, const double* src) {
+  for (int i = x.lane; i < x.cfg.D; i += 32) dst[i] = src[i];
+}
+
+// begin_update_p / end_update_p: p -= (eps/2) g  (expl_leapfrog.hpp:16-28)
+static __device__ void half_kick(const Ctx& x, double* p, const double* g, double half) {
+  for (int i = x.lane; i < x.cfg.D; i += 32) p[i] = DSUB(p[i], DMUL(half, g[i]));
+}
+
+// update_q: q += eps * invM p, then request the gradient at q.
+static __device__ void drift_and_request(const Ctx& x, double* q, const double* p,
+                                         double eps, double* req) {
+  const double* im = x.slot(SL_INVM);
+  for (int i = x.lane; i < x.cfg.D; i += 32) {
+    double v = DADD(q[i], DMUL(eps, DMUL(im[i], p[i])));
+    q[i] = v;
+    req[i] = v;
+  }
+}
+
+// V = -lp, g = -grad lp; a non-finite lp rejects the point (base_hamiltonian.hpp:61-70).
+static __device__ double take_gradient(const Ctx& x, double lp, const double* grad,
+                                       double* g) {
+  for (int i = x.lane; i < x.cfg.D; i += 32) g[i] = -grad[i];
+  if (isnan(lp)) return lp;
+  if (!isfinite(lp)) return __longlong_as_double(0x7ff0000000000000LL);
+  return -lp;
+}
+
+// constrained output (write_array): exp for the positive parameters.
+static __device__ void write_row(const Ctx& x, const ChainState& st, double* row,
+                                 double* diag) {
+  const SamplerCfg& cfg = x.cfg;
+  const double* q = x.slot(SL_SMP_Q);
+  if (x.lane == 0) {
+    row[0] = -st.V_smp;
+    row[1] = st.accept;
+    row[2] = st.eps;
+    row[3] = st.depth;
+    row[4] = st.n_lf;
+    row[5] = st.divergent;
+    row[6] = st.energy;
+  }
+  for (int i = x.lane; i < cfg.D; i += 32) {
+    double v = q[i];
+    if (i == cfg.idx_tau || i == cfg.idx_sigma) v = exp(v);
+    row[7 + i] = v;
+  }
+  if (diag) {
+    const double* p = x.slot(SL_SMP_P);
+    const double* g = x.slot(SL_SMP_G);
+    for (int i = x.lane; i < cfg.D; i += 32) {
+      diag[i] = q[i];
+      diag[cfg.D + i] = p[i];
+      diag[2 * cfg.D + i] = g[i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- adaptation
+// stepsize_adaptation::learn_stepsize (stepsize_adaptation.hpp:55-71)
+static __device__ void learn_stepsize(const SamplerCfg& cfg, ChainState& st, double stat) {
+  st.sa_counter += 1.0;
+  stat = stat > 1 ? 1 : stat;
+  const double eta = 1.0 / (st.sa_counter + cfg.t0);
+  st.sa_s_bar = DADD(DMUL(1.0 - eta, st.sa_s_bar), DMUL(eta, cfg.delta - stat));
+  const double xx = st.sa_mu - DMUL(st.sa_s_bar, sqrt(st.sa_counter)) / cfg.gamma;
+  const double x_eta = pow(st.sa_counter, -cfg.kappa);
+  st.sa_x_bar = DADD(DMUL(1.0 - x_eta, st.sa_x_bar), DMUL(x_eta, xx));
+  st.nom_eps = exp(xx);
+}
+
+// windowed_adaptation (windowed_adaptation.hpp:80-110); unsigned arithmetic.
+static __device__ bool adaptation_window(const ChainState& st) {
+  return (st.wa_counter >= st.wa_init_buffer) &&
+         (st.wa_counter < st.wa_num_warmup - st.wa_term_buffer) &&
+         (st.wa_counter != st.wa_num_warmup);
+}
+static __device__ bool end_adaptation_window(const ChainState& st) {
+  return (st.wa_counter == st.wa_next) && (st.wa_counter != st.wa_num_warmup);
+}
+static __device__ void compute_next_window(ChainState& st) {
+  const unsigned last = st.wa_num_warmup - st.wa_term_buffer - 1u;
+  if (st.wa_next == last) return;
+  st.wa_size *= 2u;
+  st.wa_next = st.wa_counter + st.wa_size;
+  if (st.wa_next == last) return;
+  unsigned boundary = st.wa_next + 2u * st.wa_size;
+  if (boundary >= st.wa_num_warmup - st.wa_term_buffer) st.wa_next = last;
+}
+
+// var_adaptation::learn_variance (var_adaptation.hpp:17-46) with Welford's
+// estimator; returns 1 on a metric update, -1 on overflow.
+static __device__ int learn_variance(const Ctx& x, ChainState& st) {
+  const int D = x.cfg.D;
+  const double* q = x.slot(SL_SMP_Q);
+  double* m = x.slot(SL_WM);
+  double* m2 = x.slot(SL_WM2);
+  double* var = x.slot(SL_INVM);
+  if (adaptation_window(st)) {
+    st.w_n += 1.0;
+    for (int i = x.lane; i < D; i += 32) {
+      double delta = DSUB(q[i], m[i]);
+      m[i] = DADD(m[i], DDIV(delta, st.w_n));
+      m2[i] = DADD(m2[i], DMUL(DSUB(q[i], m[i]), delta));
+    }
+  }
+  if (end_adaptation_window(st)) {
+    compute_next_window(st);
+    const double n = st.w_n;
+    const double a = n / (n + 5.0);
+    const double b = 1e-3 * (5.0 / (n + 5.0));
+    int bad = 0;
+    for (int i = x.lane; i < D; i += 32) {
+      double v = var[i];
+      if (n > 1) v = DDIV(m2[i], n - 1.0);
+      v = DADD(DMUL(a, v), b);
+      var[i] = v;
+      if (!isfinite(v)) bad = 1;
+      m[i] = 0.0;
+      m2[i] = 0.0;
+    }
+    st.w_n = 0.0;
+    st.wa_counter += 1u;
+    bad = __any_sync(0xffffffffu, bad);
+    return bad ? -1 : 1;
+  }
+  st.wa_counter += 1u;
+  return 0;
+}
+
+// ---------------------------------------------------------------- the machine
+// Merges the subtree `cur` (the working leaf, or stack level cur_level) into
+// stack level l (its left sibling), as build_tree does after its final
+// subtree returns (base_nuts.hpp:321-351).  Returns the U-turn verdict.
+static __device__ bool merge_into_level(const Ctx& x, ChainState& st, int l, int cur_level,
+                                        int wq, int wp, int wg, double cur_lsw, double cur_V) {
+  const SamplerCfg& cfg = x.cfg;
+  const int pi = st.slot_of[l];
+  const int base_i = SL_STACK + 6 * pi;
+  double* IQ = x.slot(base_i + 0);
+  double* IP = x.slot(base_i + 1);
+  double* IG = x.slot(base_i + 2);
+  double* IPB = x.slot(base_i + 3);
+  double* IPE = x.slot(base_i + 4);
+  double* IR = x.slot(base_i + 5);
+  const double *CQ, *CP, *CG, *CPB, *CPE, *CR;
+  if (cur_level < 0) {
+    CQ = x.slot(wq);
+    CP = x.slot(wp);
+    CG = x.slot(wg);
+    CPB = CP;
+    CPE = CP;
+    CR = CP;
+  } else {
+    const int base_c = SL_STACK + 6 * st.slot_of[cur_level];
+    CQ = x.slot(base_c + 0);
+    CP = x.slot(base_c + 1);
+    CG = x.slot(base_c + 2);
+    CPB = x.slot(base_c + 3);
+    CPE = x.slot(base_c + 4);
+    CR = x.slot(base_c + 5);
+  }
+  const double init_lsw = st.stack_lsw[l];
+  const double lsw_sub = log_sum_exp_d(init_lsw, cur_lsw);
+  bool sel_final;
+  if (cur_lsw > lsw_sub) {
+    sel_final = true;
+  } else {
+    double accept_prob = exp(cur_lsw - lsw_sub);
+    sel_final = draw_uniform(cfg, st, x.c) < accept_prob;
+  }
+  const double* im = x.slot(SL_INVM);
+  double d1a = 0, d1b = 0, d2a = 0, d2b = 0, d3a = 0, d3b = 0;
+  for (int i = x.lane; i < cfg.D; i += 32) {
+    const double ipb = IPB[i], ipe = IPE[i], ir = IR[i];
+    const double cpb = CPB[i], cpe = CPE[i], cr = CR[i];
+    const double psb = DMUL(im[i], ipb);   // p_sharp_beg
+    const double pse = DMUL(im[i], cpe);   // p_sharp_end
+    const double psie = DMUL(im[i], ipe);  // p_sharp_init_end
+    const double psfb = DMUL(im[i], cpb);  // p_sharp_final_beg
+    const double rs = DADD(ir, cr);        // rho_init + rho_final
+    const double r2 = DADD(ir, cpb);       // rho_init + p_final_beg
+    const double r3 = DADD(cr, ipe);       // rho_final + p_init_end
+    d1a += pse * rs;
+    d1b += psb * rs;
+    d2a += psfb * r2;
+    d2b += psb * r2;
+    d3a += pse * r3;
+    d3b += psie * r3;
+    IR[i] = rs;
+    IPE[i] = cpe;
+    if (sel_final) {
+      IQ[i] = CQ[i];
+      IP[i] = CP[i];
+      IG[i] = CG[i];
+    }
+  }
+  if (sel_final) st.stack_V[l] = cur_V;
+  st.stack_lsw[l] = lsw_sub;
+  d1a = warp_sum(d1a);
+  d1b = warp_sum(d1b);
+  d2a = warp_sum(d2a);
+  d2b = warp_sum(d2b);
+  d3a = warp_sum(d3a);
+  d3b = warp_sum(d3b);
+  return (d1a > 0 && d1b > 0) && (d2a > 0 && d2b > 0) && (d3a > 0 && d3b > 0);
+}
+
+// Top-level merge of a completed subtree (base_nuts.hpp:157-192).
+static __device__ bool merge_top(const Ctx& x, ChainState& st, int cur_level, int wq, int wp,
+                                 int wg, double cur_lsw, double cur_V) {
+  const SamplerCfg& cfg = x.cfg;
+  const double *CQ, *CP, *CG, *CPB, *CPE, *CR;
+  if (cur_level < 0) {
+    CQ = x.slot(wq);
+    CP = x.slot(wp);
+    CG = x.slot(wg);
+    CPB = CP;
+    CPE = CP;
+    CR = CP;
+  } else {
+    const int base_c = SL_STACK + 6 * st.slot_of[cur_level];
+    CQ = x.slot(base_c + 0);
+    CP = x.slot(base_c + 1);
+    CG = x.slot(base_c + 2);
+    CPB = x.slot(base_c + 3);
+    CPE = x.slot(base_c + 4);
+    CR = x.slot(base_c + 5);
+  }
+  st.depth += 1;
+  bool sel;
+  if (cur_lsw > st.lsw) {
+    sel = true;
+  } else {
+    double accept_prob = exp(cur_lsw - st.lsw);
+    sel = draw_uniform(cfg, st, x.c) < accept_prob;
+  }
+  st.lsw = log_sum_exp_d(st.lsw, cur_lsw);
+  double* RHO = x.slot(SL_RHO);
+  double* PFF = x.slot(SL_PFF);
+  double* PFB = x.slot(SL_PFB);
+  double* PBF = x.slot(SL_PBF);
+  double* PBB = x.slot(SL_PBB);
+  double* SQ = x.slot(SL_SMP_Q);
+  double* SP = x.slot(SL_SMP_P);
+  double* SG = x.slot(SL_SMP_G);
+  const double* im = x.slot(SL_INVM);
+  const bool fwd = st.dir > 0;
+  double d1a = 0, d1b = 0, d2a = 0, d2b = 0, d3a = 0, d3b = 0;
+  for (int i = x.lane; i < cfg.D; i += 32) {
+    double rho_bck, rho_fwd, p_ff, p_fb, p_bf, p_bb;
+    if (fwd) {
+      rho_bck = RHO[i];
+      rho_fwd = CR[i];
+      p_bf = PFF[i];
+      p_fb = CPB[i];
+      p_ff = CPE[i];
+      p_bb = PBB[i];
+    } else {
+      rho_fwd = RHO[i];
+      rho_bck = CR[i];
+      p_fb = PBB[i];
+      p_bf = CPB[i];
+      p_bb = CPE[i];
+      p_ff = PFF[i];
+    }
+    const double rho = DADD(rho_bck, rho_fwd);
+    const double ps_bb = DMUL(im[i], p_bb), ps_ff = DMUL(im[i], p_ff);
+    const double ps_fb = DMUL(im[i], p_fb), ps_bf = DMUL(im[i], p_bf);
+    const double r2 = DADD(rho_bck, p_fb);
+    const double r3 = DADD(rho_fwd, p_bf);
+    d1a += ps_ff * rho;
+    d1b += ps_bb * rho;
+    d2a += ps_fb * r2;
+    d2b += ps_bb * r2;
+    d3a += ps_ff * r3;
+    d3b += ps_bf * r3;
+    RHO[i] = rho;
+    PFF[i] = p_ff;
+    PFB[i] = p_fb;
+    PBF[i] = p_bf;
+    PBB[i] = p_bb;
+    if (sel) {
+      SQ[i] = CQ[i];
+      SP[i] = CP[i];
+      SG[i] = CG[i];
+    }
+  }
+  if (sel) st.V_smp = cur_V;
+  d1a = warp_sum(d1a);
+  d1b = warp_sum(d1b);
+  d2a = warp_sum(d2a);
+  d2b = warp_sum(d2b);
+  d3a = warp_sum(d3a);
+  d3b = warp_sum(d3b);
+  return (d1a > 0 && d1b > 0) && (d2a > 0 && d2b > 0) && (d3a > 0 && d3b > 0);
+}
+
+static __device__ void finish_chain(ChainState& st, int status, int* done_count, int lane) {
+  st.status = status;
+  st.done = 1;
+  st.phase = PH_DONE;
+  if (lane == 0) atomicAdd(done_count, 1);
+}
+
+__global__ void __launch_bounds__(128)
+    nuts_step_kernel(SamplerCfg cfg, ChainState* __restrict__ states, double* vecs,
+                     double* __restrict__ req, const double* __restrict__ lp_in,
+                     const double* __restrict__ grad_in, int* __restrict__ active,
+                     double* __restrict__ draws, double* __restrict__ diag,
+                     double* __restrict__ init_out, const double* __restrict__ inits,
+                     int* __restrict__ done_count, const int* __restrict__ abort_flag,
+                     long long step) {
+  const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= cfg.C) return;
+  ChainState st = states[c];
+  if (st.done) {
+    if (lane == 0) active[c] = 0;
+    return;
+  }
+  Ctx x{cfg, vecs, c, lane};
+  const int D = cfg.D;
+  double* rq = req + (size_t)c * cfg.ld;
+  const double* gin = grad_in + (size_t)c * cfg.ld;
+  const double lp = lp_in[c];
+  const double inf = __longlong_as_double(0x7ff0000000000000LL);
+  const double log08 = log(0.8);
+  bool yield = false;
+  int guard = 0;
+
+  while (!yield && !st.done) {
+    if (++guard > 64) {
+      finish_chain(st, GBNUTS_CHAIN_STEPSIZE_FAILED, done_count, lane);
+      break;
+    }
+    switch (st.phase) {
+      case PH_INIT_DRAW: {
+        // initialize.hpp:68-227: user values, zeros, or uniform(-R, R)
+        double* q = x.slot(SL_FWD_Q);
+        for (int i = lane; i < D; i += 32) {
+          double v;
+          if (inits)
+            v = inits[(size_t)c * D + i];
+          else if (cfg.init_radius == 0.0)
+            v = 0.0;
+          else
+            v = DMUL(DSUB(2.0 * gbds_uniform_at(cfg.seed, cfg.init_chain_id + (unsigned)c,
+                                                 st.nu + i),
+                          1.0),
+                     cfg.init_radius);
+          q[i] = v;
+          rq[i] = v;
+        }
+        if (!inits && cfg.init_radius != 0.0) st.nu += D;
+        st.phase = PH_INIT_EVAL;
+        yield = true;
+        break;
+      }
+      case PH_INIT_EVAL: {
+        st.n_grad += 1;
+        double gs = 0.0;
+        for (int i = lane; i < D; i += 32) gs += gin[i];
+        gs = warp_sum(gs);
+        if (isfinite(lp) && isfinite(gs)) {
+          copy_vec(x, x.slot(SL_SMP_Q), x.slot(SL_FWD_Q));
+          st.V_smp = take_gradient(x, lp, gin, x.slot(SL_SMP_G));
+          if (init_out) copy_vec(x, init_out + (size_t)c * D, x.slot(SL_SMP_Q));
+          if (cfg.adapt) {
+            st.ss_ctx = SS_CTX_START;
+            st.phase = PH_SS_BEGIN;
+          } else {
+            st.phase = PH_AFTER_ITER;
+          }
+        } else {
+          st.init_try += 1;
+          const int max_tries = (inits || cfg.init_radius == 0.0) ? 1 : 100;
+          if (st.init_try >= max_tries)
+            finish_chain(st, GBNUTS_CHAIN_INIT_FAILED, done_count, lane);
+          else
+            st.phase = PH_INIT_DRAW;
+        }
+        break;
+      }
+      case PH_SS_BEGIN: {
+        // base_hmc::init_stepsize (base_hmc.hpp:93-105)
+        if (st.nom_eps == 0 || st.nom_eps > 1e7 || isnan(st.nom_eps)) {
+          st.phase = PH_SS_DONE;
+          break;
+        }
+        st.ss_first = 1;
+        st.phase = PH_SS_TRIAL;
+        break;
+      }
+      case PH_SS_TRIAL: {
+        // z = z_init; sample_p; H0; evolve(nom_epsilon)  (base_hmc.hpp:107-133)
+        double* q = x.slot(SL_FWD_Q);
+        double* p = x.slot(SL_FWD_P);
+        double* g = x.slot(SL_FWD_G);
+        copy_vec(x, q, x.slot(SL_SMP_Q));
+        copy_vec(x, g, x.slot(SL_SMP_G));
+        st.V_fwd = st.V_smp;
+        sample_p(x, st, p);
+        __syncwarp();
+        st.ss_H0 = kinetic(x, p) + st.V_fwd;
+        const double e = st.nom_eps;
+        half_kick(x, p, g, 0.5 * e);
+        drift_and_request(x, q, p, e, rq);
+        st.phase = PH_SS_EVAL;
+        yield = true;
+        break;
+      }
+      case PH_SS_EVAL: {
+        st.n_grad += 1;
+        double* p = x.slot(SL_FWD_P);
+        double* g = x.slot(SL_FWD_G);
+        st.V_fwd = take_gradient(x, lp, gin, g);
+        half_kick(x, p, g, 0.5 * st.nom_eps);
+        __syncwarp();
+        double h = kinetic(x, p) + st.V_fwd;
+        if (isnan(h)) h = inf;
+        const double dH = st.ss_H0 - h;
+        if (st.ss_first) {
+          st.ss_dir = dH > log08 ? 1 : -1;
+          st.ss_first = 0;
+          st.phase = PH_SS_TRIAL;
+          break;
+        }
+        if ((st.ss_dir == 1) && !(dH > log08)) {
+          st.phase = PH_SS_DONE;
+          break;
+        }
+        if ((st.ss_dir == -1) && !(dH < log08)) {
+          st.phase = PH_SS_DONE;
+          break;
+        }
+        st.nom_eps = st.ss_dir == 1 ? 2.0 * st.nom_eps : 0.5 * st.nom_eps;
+        if (st.nom_eps > 1e7 || st.nom_eps == 0) {
+          finish_chain(st,
+                       st.ss_ctx == SS_CTX_START ? GBNUTS_CHAIN_STEPSIZE_INIT_FAILED
+                                                 : GBNUTS_CHAIN_STEPSIZE_FAILED,
+                       done_count, lane);
+          st.ss_fail = st.nom_eps > 1e7 ? 1 : 2;
+          break;
+        }
+        st.phase = PH_SS_TRIAL;
+        break;
+      }
+      case PH_SS_DONE: {
+        if (st.ss_ctx == SS_CTX_WINDOW) {
+          // adapt_diag_e_nuts.hpp:35-39
+          st.sa_mu = log(10 * st.nom_eps);
+          st.sa_counter = 0;
+          st.sa_s_bar = 0;
+          st.sa_x_bar = 0;
+        }
+        st.phase = PH_AFTER_ITER;
+        break;
+      }
+      case PH_AFTER_ITER: {
+        if (st.adapt_flag && st.iter == cfg.num_warmup) {
+          // disengage_adaptation (adapt_diag_e_nuts.hpp:45-48)
+          st.adapt_flag = 0;
+          st.nom_eps = exp(st.sa_x_bar);
+          st.warm_end_step = step;
+        } else if (!cfg.adapt && st.iter == cfg.num_warmup && st.warm_end_step < 0) {
+          st.warm_end_step = step;
+        }
+        if (st.iter >= cfg.num_warmup + cfg.num_samples) {
+          finish_chain(st, GBNUTS_CHAIN_OK, done_count, lane);
+          break;
+        }
+        if (abort_flag && *abort_flag) {
+          finish_chain(st, GBNUTS_CHAIN_INTERRUPTED, done_count, lane);
+          break;
+        }
+        st.phase = PH_TRANS_BEGIN;
+        break;
+      }
+      case PH_TRANS_BEGIN: {
+        // base_nuts::transition (base_nuts.hpp:78-121)
+        st.eps = st.nom_eps;
+        if (cfg.jitter != 0.0)
+          st.eps = DMUL(st.eps,
+                        DADD(1.0, DMUL(cfg.jitter, DSUB(2.0 * draw_uniform(cfg, st, c), 1.0))));
+        double* SP = x.slot(SL_SMP_P);
+        sample_p(x, st, SP);
+        __syncwarp();
+        const double* SQ = x.slot(SL_SMP_Q);
+        const double* SG = x.slot(SL_SMP_G);
+        double* FQ = x.slot(SL_FWD_Q);
+        double* FP = x.slot(SL_FWD_P);
+        double* FG = x.slot(SL_FWD_G);
+        double* BQ = x.slot(SL_BCK_Q);
+        double* BP = x.slot(SL_BCK_P);
+        double* BG = x.slot(SL_BCK_G);
+        double* PFF = x.slot(SL_PFF);
+        double* PFB = x.slot(SL_PFB);
+        double* PBF = x.slot(SL_PBF);
+        double* PBB = x.slot(SL_PBB);
+        double* RHO = x.slot(SL_RHO);
+        for (int i = lane; i < D; i += 32) {
+          const double q = SQ[i], p = SP[i], g = SG[i];
+          FQ[i] = q;
+          FP[i] = p;
+          FG[i] = g;
+          BQ[i] = q;
+          BP[i] = p;
+          BG[i] = g;
+          PFF[i] = p;
+          PFB[i] = p;
+          PBF[i] = p;
+          PBB[i] = p;
+          RHO[i] = p;
+        }
+        st.V_fwd = st.V_smp;
+        st.V_bck = st.V_smp;
+        st.H0 = kinetic(x, SP) + st.V_smp;
+        st.lsw = 0.0;
+        st.n_lf = 0;
+        st.sum_metro = 0.0;
+        st.depth = 0;
+        st.divergent = 0;
+        st.phase = PH_DOUBLING;
+        break;
+      }
+      case PH_DOUBLING: {
+        if (st.depth >= cfg.max_depth) {
+          st.phase = PH_TRANS_END;
+          break;
+        }
+        st.dir = draw_uniform(cfg, st, c) > 0.5 ? 1 : -1;
+        st.sub_d = st.depth;
+        st.leaf = 0;
+        for (int l = 0; l < MAX_TREE_DEPTH; ++l) st.slot_of[l] = (unsigned char)l;
+        st.phase = PH_LEAF_BEGIN;
+        break;
+      }
+      case PH_LEAF_BEGIN: {
+        const bool fwd = st.dir > 0;
+        double* q = x.slot(fwd ? SL_FWD_Q : SL_BCK_Q);
+        double* p = x.slot(fwd ? SL_FWD_P : SL_BCK_P);
+        const double* g = x.slot(fwd ? SL_FWD_G : SL_BCK_G);
+        const double e = st.dir * st.eps;
+        half_kick(x, p, g, 0.5 * e);
+        drift_and_request(x, q, p, e, rq);
+        st.phase = PH_LEAF_EVAL;
+        yield = true;
+        break;
+      }
+      case PH_LEAF_EVAL: {
+        st.n_grad += 1;
+        const bool fwd = st.dir > 0;
+        const int wq = fwd ? SL_FWD_Q : SL_BCK_Q;
+        const int wp = fwd ? SL_FWD_P : SL_BCK_P;
+        const int wg = fwd ? SL_FWD_G : SL_BCK_G;
+        double* p = x.slot(wp);
+        double* g = x.slot(wg);
+        const double V = take_gradient(x, lp, gin, g);
+        if (fwd)
+          st.V_fwd = V;
+        else
+          st.V_bck = V;
+        const double e = st.dir * st.eps;
+        half_kick(x, p, g, 0.5 * e);
+        __syncwarp();
+        // leaf of build_tree (base_nuts.hpp:253-281)
+        st.n_lf += 1;
+        double h = kinetic(x, p) + V;
+        if (isnan(h)) h = inf;
+        if ((h - st.H0) > 1000.0) st.divergent = 1;
+        const double w = st.H0 - h;
+        if (w > 0)
+          st.sum_metro += 1;
+        else
+          st.sum_metro += exp(w);
+        if (st.divergent) {
+          st.phase = PH_TRANS_END;
+          break;
+        }
+        const int d = st.sub_d;
+        const int i = st.leaf;
+        int l = 0;
+        int cur_level = -1;
+        double cur_lsw = w;
+        double cur_V = V;
+        bool ok = true;
+        while (l < d && ((i >> l) & 1)) {
+          __syncwarp();
+          ok = merge_into_level(x, st, l, cur_level, wq, wp, wg, cur_lsw, cur_V);
+          cur_level = l;
+          cur_lsw = st.stack_lsw[l];
+          cur_V = st.stack_V[l];
+          ++l;
+          if (!ok) break;
+        }
+        if (!ok) {
+          st.phase = PH_TRANS_END;
+          break;
+        }
+        if (l < d) {
+          if (cur_level < 0) {
+            // push the leaf as the left sibling at level 0
+            const int base_i = SL_STACK + 6 * st.slot_of[0];
+            double* IQ = x.slot(base_i + 0);
+            double* IP = x.slot(base_i + 1);
+            double* IG = x.slot(base_i + 2);
+            double* IPB = x.slot(base_i + 3);
+            double* IPE = x.slot(base_i + 4);
+            double* IR = x.slot(base_i + 5);
+            const double* Q = x.slot(wq);
+            for (int k = lane; k < D; k += 32) {
+              const double pk = p[k];
+              IQ[k] = Q[k];
+              IP[k] = pk;
+              IG[k] = g[k];
+              IPB[k] = pk;
+              IPE[k] = pk;
+              IR[k] = pk;
+            }
+            st.stack_lsw[0] = w;
+            st.stack_V[0] = V;
+          } else {
+            // the merged subtree at level l-1 becomes the left sibling at level l
+            unsigned char t = st.slot_of[l];
+            st.slot_of[l] = st.slot_of[l - 1];
+            st.slot_of[l - 1] = t;
+            st.stack_lsw[l] = st.stack_lsw[l - 1];
+            st.stack_V[l] = st.stack_V[l - 1];
+          }
+          st.leaf += 1;
+          st.phase = PH_LEAF_BEGIN;
+          break;
+        }
+        __syncwarp();
+        const bool persist = merge_top(x, st, cur_level, wq, wp, wg, cur_lsw, cur_V);
+        st.phase = persist ? PH_DOUBLING : PH_TRANS_END;
+        break;
+      }
+      case PH_TRANS_END: {
+        // base_nuts.hpp:195-203, then generate_transitions' write and
+        // adapt_diag_e_nuts' learning
+        __syncwarp();
+        st.accept = st.sum_metro / (double)st.n_lf;
+        st.energy = kinetic(x, x.slot(SL_SMP_P)) + st.V_smp;
+        const int m = st.iter;
+        bool save;
+        if (m < cfg.num_warmup)
+          save = cfg.save_warmup && (m % cfg.num_thin) == 0;
+        else
+          save = ((m - cfg.num_warmup) % cfg.num_thin) == 0;
+        if (save && st.rows < cfg.max_rows) {
+          double* row = draws + ((size_t)c * cfg.max_rows + st.rows) * cfg.n_cols;
+          double* dg = diag ? diag + ((size_t)c * cfg.max_rows + st.rows) * 3 * D : nullptr;
+          write_row(x, st, row, dg);
+          st.rows += 1;
+          if (m < cfg.num_warmup) st.warm_rows += 1;
+        }
+        st.iter += 1;
+        st.phase = PH_AFTER_ITER;
+        if (st.adapt_flag) {
+          learn_stepsize(cfg, st, st.accept);
+          __syncwarp();
+          const int upd = learn_variance(x, st);
+          if (upd < 0) {
+            finish_chain(st, GBNUTS_CHAIN_METRIC_OVERFLOW, done_count, lane);
+            break;
+          }
+          if (upd > 0) {
+            st.ss_ctx = SS_CTX_WINDOW;
+            st.phase = PH_SS_BEGIN;
+          }
+        }
+        break;
+      }
+      default:
+        finish_chain(st, GBNUTS_CHAIN_STEPSIZE_FAILED, done_count, lane);
+        break;
+    }
+    __syncwarp();
+  }
+  __syncwarp();
+  if (lane == 0) {
+    states[c] = st;
+    active[c] = (yield && !st.done) ? 1 : 0;
+  }
+}
+
+// Sets every chain's state from the configuration (service set-up,
+// hmc_nuts_diag_e_adapt.hpp:360-381).
+__global__ void nuts_init_kernel(SamplerCfg cfg, ChainState* states, double* vecs,
+                                 const double* inv_metrics, int* active, double* lp_in) {
+  const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= cfg.C) return;
+  for (int s = 0; s < cfg.n_slots; ++s) {
+    double* v = vecs + ((size_t)c * cfg.n_slots + s) * cfg.ld;
+    for (int i = lane; i < cfg.ld; i += 32)
+      v[i] = (s == SL_INVM) ? (inv_metrics ? (i < cfg.D ? inv_metrics[(size_t)c * cfg.D + i] : 1.0)
+                                           : 1.0)
+                            : 0.0;
+  }
+  if (lane == 0) {
+    ChainState st;
+    memset(&st, 0, sizeof(st));
+    st.phase = PH_INIT_DRAW;
+    st.nom_eps = cfg.stepsize;
+    st.eps = cfg.stepsize;
+    st.sa_mu = log(10 * cfg.stepsize);
+    st.adapt_flag = cfg.adapt;
+    st.wa_num_warmup = cfg.wa_num_warmup;
+    st.wa_init_buffer = cfg.wa_init_buffer;
+    st.wa_term_buffer = cfg.wa_term_buffer;
+    st.wa_base_window = cfg.wa_base_window;
+    st.wa_counter = 0;
+    st.wa_size = cfg.wa_size0;
+    st.wa_next = cfg.wa_next0;
+    st.warm_end_step = -1;
+    for (int l = 0; l < MAX_TREE_DEPTH; ++l) st.slot_of[l] = (unsigned char)l;
+    states[c] = st;
+    active[c] = 0;
+    lp_in[c] = 0.0;
+  }
+}
+
+void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, double* vecs,
+                      const double* inv_metrics, int* active, double* lp_in,
+                      cudaStream_t s) {
+  const int threads = 128;
+  const int blocks = (int)(((size_t)cfg.C * 32 + threads - 1) / threads);
+  nuts_init_kernel<<<blocks, threads, 0, s>>>(cfg, states, vecs, inv_metrics, active, lp_in);
+}
+
+void launch_nuts_step(const SamplerCfg& cfg, ChainState* states, double* vecs, double* req,
+                      const double* lp_in, const double* grad_in, int* active,
+                      double* draws, double* diag, double* init_out, const double* inits,
+                      int* done_count, const int* abort_flag, long long step,
+                      cudaStream_t s) {
+  const int threads = 128;
+  const int blocks = (int)(((size_t)cfg.C * 32 + threads - 1) / threads);
+  nuts_step_kernel<<<blocks, threads, 0, s>>>(cfg, states, vecs, req, lp_in, grad_in, active,
+                                              draws, diag, init_out, inits, done_count,
+                                              abort_flag, step);
+}
+
+}  // namespace gbn

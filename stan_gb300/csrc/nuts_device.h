@@ -1,0 +1,72 @@
+// Per-chain sampler state of the device NUTS state machine.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbn {
+
+constexpr int MAX_TREE_DEPTH = 16;
+
+// Vector slots of a chain (each `ld` doubles): the two trajectory ends (the
+// end being extended is integrated in place), the current sample, the momenta
+// at the inner and outer edge of the forward and backward halves, the summed
+// momentum, the inverse metric, the Welford accumulators, then 6 slots per
+// stack level (proposal q, p, g; momentum at the subtree's first and last
+// leaf; summed momentum).
+enum Slot {
+  SL_FWD_Q = 0, SL_FWD_P, SL_FWD_G,
+  SL_BCK_Q, SL_BCK_P, SL_BCK_G,
+  SL_SMP_Q, SL_SMP_P, SL_SMP_G,
+  SL_PFF, SL_PFB, SL_PBF, SL_PBB,
+  SL_RHO, SL_INVM, SL_WM, SL_WM2,
+  SL_STACK
+};
+
+enum Phase {
+  PH_INIT_DRAW = 0, PH_INIT_EVAL, PH_SS_BEGIN, PH_SS_TRIAL, PH_SS_EVAL, PH_SS_DONE,
+  PH_AFTER_ITER, PH_TRANS_BEGIN, PH_DOUBLING, PH_LEAF_BEGIN, PH_LEAF_EVAL, PH_TRANS_END,
+  PH_DONE
+};
+
+enum { SS_CTX_START = 0, SS_CTX_WINDOW = 1 };
+
+struct SamplerCfg {
+  int C, D, ld, n_slots, max_depth;
+  int adapt, num_warmup, num_samples, num_thin, save_warmup;
+  int max_rows, n_cols;
+  double stepsize, jitter, delta, gamma, kappa, t0, init_radius;
+  unsigned wa_num_warmup, wa_init_buffer, wa_term_buffer, wa_base_window;
+  unsigned wa_size0, wa_next0;  // window size and end after set_window_params
+  unsigned seed, init_chain_id;
+  int idx_tau, idx_sigma;
+};
+
+struct ChainState {
+  int phase, status, done, iter, init_try;
+  int depth, n_lf, divergent, dir, sub_d, leaf;
+  int ss_ctx, ss_dir, ss_first, ss_fail;
+  int rows, warm_rows, adapt_flag;
+  unsigned long long nu, nn;  // uniforms and normals consumed
+  long long n_grad, warm_end_step;
+  double nom_eps, eps, H0, lsw, sum_metro, accept, energy;
+  double V_fwd, V_bck, V_smp, ss_H0;
+  double sa_counter, sa_s_bar, sa_x_bar, sa_mu;
+  unsigned wa_num_warmup, wa_init_buffer, wa_term_buffer, wa_base_window;
+  unsigned wa_counter, wa_next, wa_size;
+  double w_n;
+  double stack_lsw[MAX_TREE_DEPTH];
+  double stack_V[MAX_TREE_DEPTH];
+  unsigned char slot_of[MAX_TREE_DEPTH];
+};
+
+void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, double* vecs,
+                      const double* inv_metrics, int* active, double* lp_in,
+                      cudaStream_t s);
+void launch_nuts_step(const SamplerCfg& cfg, ChainState* states, double* vecs, double* req,
+                      const double* lp_in, const double* grad_in, int* active,
+                      double* draws, double* diag, double* init_out, const double* inits,
+                      int* done_count, const int* abort_flag, long long step,
+                      cudaStream_t s);
+
+}  // namespace gbn

@@ -1,0 +1,81 @@
+"""Array interface to the device run (gbnuts_sample_run): draws as NumPy arrays."""
+import ctypes
+import dataclasses
+
+import numpy as np
+
+from . import _lib
+
+SAMPLER_COLUMNS = ["lp__", "accept_stat__", "stepsize__", "treedepth__", "n_leapfrog__",
+                   "divergent__", "energy__"]
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+@dataclasses.dataclass
+class RunResult:
+    draws: np.ndarray        # (chains, rows, 7 + D); rows beyond n_rows are zero
+    n_rows: np.ndarray
+    n_warmup_rows: np.ndarray
+    status: np.ndarray
+    stepsize: np.ndarray
+    inv_metric: np.ndarray
+    init: np.ndarray
+    n_grad: np.ndarray
+    seconds: np.ndarray
+    total_ms: float
+    grad_ms: float           # mean duration of one batched-gradient partial kernel
+    steps: int
+    kernel_launches: int
+    diagnostics: np.ndarray = None
+
+    def sampling_draws(self):
+        """(iterations, chains, 7 + D) post-warmup draws (the chainset layout)."""
+        w = int(self.n_warmup_rows.max()) if self.n_warmup_rows.size else 0
+        n = int(self.n_rows.min())
+        return np.transpose(self.draws[:, w:n], (1, 0, 2))
+
+
+def run(model, num_chains=4, adapt=True, num_warmup=1000, num_samples=1000, num_thin=1,
+        save_warmup=False, stepsize=1.0, stepsize_jitter=0.0, max_depth=10, delta=0.8,
+        gamma=0.05, kappa=0.75, t0=10.0, init_buffer=75, term_buffer=50, window=25,
+        init_radius=2.0, random_seed=0, init_chain_id=1, precision="fp64",
+        inits=None, inv_metrics=None, save_diagnostics=False):
+    lib = _lib.load()
+    C, D = num_chains, model.D
+    prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
+    ini = None if inits is None else np.ascontiguousarray(inits, dtype=np.float64).reshape(C, D)
+    imi = None if inv_metrics is None else np.ascontiguousarray(inv_metrics, dtype=np.float64).reshape(C, D)
+    cfg = _lib.RunConfig(C, int(adapt), num_warmup, num_samples, num_thin, int(save_warmup),
+                         stepsize, stepsize_jitter, max_depth, delta, gamma, kappa, t0,
+                         init_buffer, term_buffer, window, init_radius, random_seed,
+                         init_chain_id, prec, int(save_diagnostics),
+                         None if ini is None else _ptr(ini), None if imi is None else _ptr(imi))
+    rows = ((num_warmup + num_thin - 1) // num_thin if save_warmup else 0) + \
+        (num_samples + num_thin - 1) // num_thin
+    rows = max(rows, 1)
+    ncol = 7 + D
+    draws = np.zeros((C, rows, ncol))
+    diag = np.zeros((C, rows, 3 * D)) if save_diagnostics else None
+    n_rows = np.zeros(C, dtype=np.int32)
+    n_warm = np.zeros(C, dtype=np.int32)
+    status = np.zeros(C, dtype=np.int32)
+    eps = np.zeros(C)
+    invm = np.zeros((C, D))
+    init = np.zeros((C, D))
+    ngrad = np.zeros(C, dtype=np.int64)
+    secs = np.zeros((C, 2))
+    out = _lib.RunOutput(rows, ncol, _ptr(draws), None if diag is None else _ptr(diag),
+                         n_rows.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                         n_warm.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                         status.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                         _ptr(eps), _ptr(invm), _ptr(init),
+                         ngrad.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), _ptr(secs),
+                         0.0, 0.0, 0, 0)
+    rc = lib.gbnuts_sample_run(model.handle, ctypes.byref(cfg), ctypes.byref(out), None)
+    _lib.check(rc, "gbnuts_sample_run")
+    return RunResult(draws, n_rows, n_warm, status, eps, invm, init, ngrad, secs,
+                     out.total_ms, out.grad_ms, out.steps, out.kernel_launches, diag)

@@ -1,0 +1,109 @@
+"""Batched log density and gradient on the GPU against the FP64 oracle.
+
+Tolerances: FP64 form <= 1e-12 relative (lp; gradient in the max norm);
+FP32 form: gradient <= 1e-4 relative in the 2-norm, lp <= 1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+from tests.datasets import make_dataset
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["logistic", "logistic_100k", "poisson", "hier_normal", "hier_logistic"]
+
+
+@pytest.fixture(scope="module")
+def models():
+    from stan_gb300 import Model
+    out = {}
+    for kind in KINDS:
+        ds = make_dataset(kind, small=True, seed=7)
+        out[kind] = (ds, Model.from_dataset(ds), ds.oracle_model())
+    return out
+
+
+def _points(D, C, seed, scale=0.3):
+    return np.random.default_rng(seed).normal(size=(C, D)) * scale
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_fp64_single_point_matches_oracle(models, kind):
+    ds, m, om = models[kind]
+    for th in _points(m.D, 4, 1):
+        for propto in (True, False):
+            for jac in (True, False):
+                lp, g = m.log_prob_grad(th, propto=propto, jacobian=jac)
+                lpo, go = om.log_prob_grad(th, propto=propto, jacobian=jac)
+                assert abs(lp - lpo) <= 1e-12 * max(1.0, abs(lpo))
+                assert np.max(np.abs(g - go)) <= 1e-12 * max(1.0, np.max(np.abs(go)))
+                assert m.log_prob(th, propto=propto, jacobian=jac) == pytest.approx(lp, rel=1e-15, abs=1e-15)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_fp64_batch_matches_oracle(models, kind):
+    ds, m, om = models[kind]
+    C = 37
+    th = _points(m.D, C, 2)
+    lp, g = m.log_prob_grad_batch(th, "fp64")
+    for c in range(C):
+        lpo, go = om.log_prob_grad(th[c])
+        assert abs(lp[c] - lpo) <= 1e-12 * max(1.0, abs(lpo))
+        assert np.max(np.abs(g[c] - go)) <= 1e-12 * max(1.0, np.max(np.abs(go)))
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_fp32_batch_within_stated_tolerance(models, kind):
+    ds, m, om = models[kind]
+    C = 19
+    th = _points(m.D, C, 3)
+    lp, g = m.log_prob_grad_batch(th, "fp32")
+    for c in range(C):
+        lpo, go = om.log_prob_grad(th[c])
+        assert abs(lp[c] - lpo) <= 1e-5 * abs(lpo)
+        assert np.linalg.norm(g[c] - go) <= 1e-4 * np.linalg.norm(go)
+
+
+def test_full_size_logistic_batch():
+    """N = 100000, K = 100 (X stored FP32): FP64 batch vs oracle at 8 points."""
+    from stan_gb300 import Model
+    ds = make_dataset("logistic_100k", small=False, seed=1)
+    m = Model.from_dataset(ds)
+    om = ds.oracle_model()
+    th = _points(m.D, 8, 4, scale=0.05)
+    lp, g = m.log_prob_grad_batch(th, "fp64")
+    lp32, g32 = m.log_prob_grad_batch(th, "fp32")
+    for c in range(8):
+        lpo, go = om.log_prob_grad(th[c])
+        assert abs(lp[c] - lpo) <= 1e-12 * abs(lpo)
+        assert np.max(np.abs(g[c] - go)) <= 1e-12 * np.max(np.abs(go))
+        assert np.linalg.norm(g32[c] - go) <= 1e-4 * np.linalg.norm(go)
+
+
+def test_group_sums_with_single_row_groups_and_large_groups():
+    """Segmented group reduction across tile and chunk boundaries."""
+    from stan_gb300 import Model
+    from stan_gb300.workloads import Dataset, HIER_NORMAL
+    rng = np.random.default_rng(5)
+    sizes = np.array([1, 1, 300, 2, 31, 32, 33, 64, 65, 1, 500, 7])
+    J = sizes.size
+    g = np.repeat(np.arange(J, dtype=np.int32), sizes)
+    N, K = g.size, 3
+    X = rng.normal(size=(N, K))
+    y = rng.normal(size=N)
+    ds = Dataset("groups", HIER_NORMAL, X, y, "f64", group=g, J=J, hp=(5.0, 1.0, 1.0, 1.0))
+    m = Model.from_dataset(ds)
+    om = ds.oracle_model()
+    th = _points(m.D, 5, 6)
+    lp, gr = m.log_prob_grad_batch(th, "fp64")
+    for c in range(5):
+        lpo, go = om.log_prob_grad(th[c])
+        assert abs(lp[c] - lpo) <= 1e-12 * abs(lpo)
+        assert np.max(np.abs(gr[c] - go)) <= 1e-12 * np.max(np.abs(go))
+
+
+def test_non_finite_density_is_reported_not_raised(models):
+    ds, m, om = models["poisson"]
+    th = np.full(m.D, 400.0)
+    lp, g = m.log_prob_grad(th)
+    assert not np.isfinite(lp)
