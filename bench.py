@@ -1,0 +1,351 @@
+"""Benchmark: NUTS (diag_e, adaptive) on the 1024-chain logistic GLM.
+
+Workload (one step = one complete fit): Bayesian logistic regression,
+N = 100000 rows, K = 100 predictors, X ~ N(0,1) with standardised columns
+stored FP32, alpha, beta ~ N(0, 2.5) priors; 1024 chains in one device run,
+500 warmup + 1000 sampling iterations, max tree depth 10, delta 0.8.
+Synthetic seeded data (no public dataset is named for this path).
+
+value       : whole-job gradient evaluations per second (sum over chains of
+              leapfrog steps + step-size search trials + init evaluations,
+              divided by the device time of the fits, CUDA events).
+extra keys  : min bulk ESS/s of the fit (split rank-normalised bulk ESS over
+              all parameters and lp__), ESS per gradient evaluation, the
+              gradient kernel's roofline, the FP64 form's gradient rate,
+              the CPU baseline.
+e2e         : the same metric through the C ABI with host buffers (model
+              creation with the H2D copy of X and y, the fit, and the D2H copy
+              of every draw inside the timed region).
+
+--impl reference runs the CPU restatement of the reference's sampler (the
+reference itself cannot be built here) on all host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "logistic_100k": dict(kind="logistic_100k", chains=1024, warmup=500, samples=1000),
+    "logistic_1k": dict(kind="logistic", chains=4, warmup=1000, samples=1000),
+    "hier_normal": dict(kind="hier_normal", chains=256, warmup=500, samples=1000),
+    "poisson_262k": dict(kind="poisson", chains=512, warmup=500, samples=1000),
+}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2(lib_module=None):
+    """Writes a 256 MiB device buffer (twice the 129 MB L2) between timed fits."""
+    import ctypes
+    cudart = ctypes.CDLL("libcudart.so")
+    p = ctypes.c_void_p()
+    n = 256 << 20
+    if cudart.cudaMalloc(ctypes.byref(p), ctypes.c_size_t(n)) == 0:
+        cudart.cudaMemset(p, 1, ctypes.c_size_t(n))
+        cudart.cudaDeviceSynchronize()
+        cudart.cudaFree(p)
+
+
+def fit_stats(res, ds):
+    from stan_gb300 import analyze
+    grads = int(res.n_grad.sum())
+    secs = res.total_ms / 1e3
+    draws = res.sampling_draws()  # (iters, chains, 7 + D)
+    q = np.concatenate([draws[:, :, 0:1], draws[:, :, 7:]], axis=2)
+    ess, which = analyze.min_bulk_ess(q, ["lp__"] + ds.param_names())
+    return grads, secs, ess, which
+
+
+def cpu_baseline(ds, wl, seconds_target=20.0, stepsize=None, inv_metric=None):
+    """The oracle (plain FP64 sums, the reference's algorithm) on all host cores:
+    one chain per core, non-adaptive NUTS at the GPU-adapted step size and
+    metric, timed until ~seconds_target of work; gradient evaluations per
+    second counts every evaluation (including the recompute at each
+    transition start that the reference performs)."""
+    import oracle
+    cores = os.cpu_count() or 1
+    om = oracle.OracleModel(ds.kind, ds.X, ds.y, group=ds.group, J=ds.J, hp=list(ds.hp),
+                            intercept=ds.intercept, compensated=False)
+    C = cores
+    kw = dict(num_chains=C, adapt=False, num_warmup=0, max_depth=10, seed=99,
+              stepsize=stepsize if stepsize else 0.05, init_radius=0.5, num_threads=cores)
+    if inv_metric is not None:
+        kw["inv_metrics"] = np.tile(inv_metric, (C, 1))
+    # calibrate with a short run, then size the sample to ~seconds_target
+    t0 = time.time()
+    r = om.sample(num_samples=2, **kw)
+    t1 = time.time()
+    g = int(r["n_grad_total"].sum())
+    rate = g / max(t1 - t0, 1e-9)
+    per_transition = max(g / (2 * C), 1)
+    n = int(max(2, min(2000, seconds_target * rate / (per_transition * C))))
+    t0 = time.time()
+    r = om.sample(num_samples=n, **kw)
+    dt = time.time() - t0
+    g = int(r["n_grad_total"].sum())
+    return {"value": g / dt, "unit": "grad evals/s", "cores": cores, "kind": "port",
+            "sample": f"{C} chains x {n} non-adaptive NUTS transitions of the same posterior "
+                      f"(one chain per core, FP64, {g} gradient evaluations in {dt:.1f} s)"}
+
+
+def run_ours(args, ws, rank, local):
+    from stan_gb300 import Model, _lib, sampler, workloads
+    wl = WORKLOADS[args.workload]
+    ds = workloads.make_dataset(wl["kind"], seed=1 + rank)
+    _lib.load(build_if_missing=False)
+    model = Model.from_dataset(ds)
+    C = wl["chains"]
+    kw = dict(num_chains=C, num_warmup=wl["warmup"], num_samples=wl["samples"], adapt=True,
+              max_depth=10, delta=0.8, precision=args.precision, init_radius=2.0)
+    for i in range(args.warmup):
+        sampler.run(model, random_seed=1000 + i, **kw)
+    barrier(ws)
+    grads_total, secs_total = 0, 0.0
+    last = None
+    grad_ms = []
+    steps = 0
+    launches = 0
+    with ClockSampler(local) as clk:
+        t_wall = time.time()
+        for i in range(args.steps):
+            flush_l2()
+            res = sampler.run(model, random_seed=2000 + i, **kw)
+            grads_total += int(res.n_grad.sum())
+            secs_total += res.total_ms / 1e3
+            grad_ms.append(res.grad_ms)
+            steps += res.steps
+            launches += res.kernel_launches
+            last = res
+        wall = time.time() - t_wall
+    secs_total = max_over_ranks(secs_total, ws)
+    grads_all = sum_over_ranks(grads_total, ws)
+    value = grads_all / secs_total
+    g, s, ess, which = fit_stats(last, ds)
+    ess_per_s = ess / s
+    # roofline of the batched gradient kernel (dominant): 4 N K C flops per launch
+    N, K = ds.N, ds.K
+    flops = 4.0 * N * K * C
+    mean_ms = float(np.mean(grad_ms))
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    if args.precision == "fp64":
+        bound, peak, unit, ach = "tensor", peaks.get("bf16_tflops", 1900.0), "TFLOP/s", flops / (mean_ms * 1e-3) / 1e12
+    else:
+        bound, peak, unit, ach = "tensor", peaks.get("bf16_tflops", 1900.0), "TFLOP/s", flops / (mean_ms * 1e-3) / 1e12
+    roof = {"bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
+            "traffic": None, "kernel": "loglik_partial_kernel", "mean_launch_ms": mean_ms,
+            "flops_per_launch": flops}
+    out = {"metric": "grad evals/s", "value": value, "unit": "grad evals/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": secs_total * 1e3 / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+           "data": "synthetic (seeded; shapes and distributions of the workload)",
+           "config": {"workload": f"{args.workload}: logistic GLM N={N} K={K} X fp32, {C} chains, "
+                                  f"{wl['warmup']} warmup + {wl['samples']} draws, max_depth 10",
+                      "precision": args.precision, "parallelism": f"replicas x{ws}",
+                      "l2": "256 MiB buffer written between timed fits"},
+           "min_bulk_ess_per_s": ess_per_s, "min_bulk_ess": ess, "min_ess_param": which,
+           "ess_per_grad": ess / g, "fit_seconds": s, "device_steps": steps,
+           "roofline": roof, "gpu_launches": int(launches), "clocks": clk.summary(),
+           "wall_seconds_timed": wall}
+    if rank == 0 and not args.no_e2e:
+        out["e2e"] = e2e(args, ds, kw)
+    if rank == 0 and not args.no_fp64:
+        out["fp64_form"] = fp64_rate(model, ds, C)
+    if rank == 0 and not args.no_cpu:
+        eps = float(np.median(last.stepsize))
+        out["cpu_baseline"] = cpu_baseline(ds, wl, args.cpu_seconds, eps,
+                                           np.median(last.inv_metric, axis=0))
+    return out
+
+
+def e2e(args, ds, kw):
+    """Through the C ABI with host buffers: H2D of X and y (model creation),
+    the fit, and the D2H copy of all draws, timed on the host."""
+    from stan_gb300 import Model, sampler
+    t0 = time.time()
+    grads = 0
+    d2h = 0
+    for i in range(args.steps):
+        m = Model.from_dataset(ds)
+        res = sampler.run(m, random_seed=3000 + i, **kw)
+        grads += int(res.n_grad.sum())
+        d2h += res.draws.nbytes
+        m.close()
+    dt = time.time() - t0
+    h2d = ds.N * ds.K * 4 + ds.N * 8
+    return {"value": grads / dt, "unit": "grad evals/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h // max(args.steps, 1)}
+
+
+def fp64_rate(model, ds, C):
+    """The plain FP64 form on the same workload: gradient evaluations per
+    second over a bounded prefix of the fit (its warmup), not a full fit."""
+    from stan_gb300 import sampler
+    res = sampler.run(model, num_chains=C, num_warmup=20, num_samples=0, adapt=True,
+                      precision="fp64", random_seed=7, init_radius=2.0)
+    return {"grad_evals_per_s": float(res.n_grad.sum()) / (res.total_ms / 1e3),
+            "sample": f"{C} chains x 20 warmup iterations", "grad_kernel_ms": res.grad_ms}
+
+
+def run_reference(args, ws, rank):
+    from stan_gb300 import workloads
+    wl = WORKLOADS[args.workload]
+    ds = workloads.make_dataset(wl["kind"], seed=1)
+    for _ in range(args.warmup):
+        cpu_baseline(ds, wl, 2.0, 0.02)
+    vals, samples = [], None
+    for _ in range(args.steps):
+        r = cpu_baseline(ds, wl, args.cpu_seconds, 0.02)
+        vals.append(r["value"])
+        samples = r
+    v = float(np.mean(vals))
+    return {"impl": "reference", "metric": "grad evals/s", "value": v, "unit": "grad evals/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload,
+                       "note": "the reference cannot be built here (Stan Math, Eigen, Boost absent); "
+                               "its sampler is timed through the CPU restatement in oracle/"},
+            "cpu_baseline": {"value": v, "unit": "grad evals/s", "cores": samples["cores"],
+                             "kind": "port", "sample": samples["sample"]},
+            "e2e": {"value": v, "unit": "grad evals/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+_dist = None
+
+
+def _init_dist(ws):
+    global _dist
+    if ws > 1 and _dist is None:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        _dist = dist
+    return _dist
+
+
+def barrier(ws):
+    d = _init_dist(ws)
+    if d:
+        d.barrier()
+
+
+def max_over_ranks(x, ws):
+    d = _init_dist(ws)
+    if not d:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    d.all_reduce(t, op=d.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, ws):
+    d = _init_dist(ws)
+    if not d:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    d.all_reduce(t, op=d.ReduceOp.SUM)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="logistic_100k", choices=list(WORKLOADS))
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "bf16x3"])
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args, ws, rank)))
+        return
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if ws > 1 else None
+    out = run_ours(args, ws, rank, local)
+    if rank == 0:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

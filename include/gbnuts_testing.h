@@ -1,0 +1,23 @@
+/*
+ * Test hooks of the gbnuts library.  They have no counterpart in the
+ * reference; they exist so the tests can check device building blocks in
+ * isolation.
+ */
+#ifndef GBNUTS_TESTING_H
+#define GBNUTS_TESTING_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One tile through the tensor-core contraction layouts used by the bf16x3
+ * gradient: D1 = A . B^T and D2 = A^T . R with A 128x128, B 64x128 and
+ * R 128x64 bf16 matrices (row-major uint16 bit patterns), D1 and D2 128x64
+ * fp32 outputs.  Returns 0 on success. */
+int gbnuts_tc_probe(const uint16_t* A, const uint16_t* B, const uint16_t* R, float* D1,
+                    float* D2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

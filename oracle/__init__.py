@@ -54,6 +54,7 @@ class _ChainOut(ctypes.Structure):
         ("n_saved", ctypes.POINTER(ctypes.c_int)), ("return_code", ctypes.POINTER(ctypes.c_int)),
         ("seconds", ctypes.POINTER(ctypes.c_double)),
         ("draws_used", ctypes.POINTER(ctypes.c_ulonglong)),
+        ("n_grad_total", ctypes.POINTER(ctypes.c_longlong)),
     ]
 
 
@@ -156,6 +157,7 @@ class OracleModel:
         rc = np.zeros(C, dtype=np.int32)
         secs = np.zeros((C, 2))
         used = np.zeros((C, 2), dtype=np.uint64)
+        ngt = np.zeros(C, dtype=np.int64)
         outs = (_ChainOut * C)()
         for i in range(C):
             outs[i] = _ChainOut(
@@ -165,7 +167,8 @@ class OracleModel:
                 ns[i:i + 1].ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                 rc[i:i + 1].ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                 _dp(secs[i]),
-                used[i].ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)))
+                used[i].ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)),
+                ngt[i:i + 1].ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
         ini = None if inits is None else np.ascontiguousarray(inits, dtype=np.float64).reshape(C, D)
         imi = None if inv_metrics is None else np.ascontiguousarray(inv_metrics, dtype=np.float64).reshape(C, D)
         nt = num_threads or os.cpu_count() or 1
@@ -175,7 +178,7 @@ class OracleModel:
         return {
             "rows": rows[:, :m], "unc": unc[:, :m], "init": init, "inv_metric": im,
             "stepsize": eps, "n_grad": ng, "n_saved": ns, "return_code": rc,
-            "seconds": secs, "draws_used": used,
+            "seconds": secs, "draws_used": used, "n_grad_total": ngt,
         }
 
 

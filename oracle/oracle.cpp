@@ -910,6 +910,7 @@ struct ChainOut {
   double stepsize = 0;
   Vec inv_metric;
   long long n_grad = 0;
+  long long n_grad_total = 0;  // every evaluation, incl. the transition-start recompute
   int n_saved = 0;
   int n_warmup_saved = 0;
   int return_code = 0;
@@ -1062,6 +1063,7 @@ static void run_chain(const Model& m, const SamplerConfig& cfg, const double* in
     out.return_code = 70;
   }
   out.n_grad += sampler.n_stepsize_trials + sampler.total_leapfrogs;
+  out.n_grad_total = ham.n_grad + out.n_grad - sampler.n_stepsize_trials - sampler.total_leapfrogs;
   out.n_uniform = rng.n_uniform;
   out.n_normal = rng.n_normal;
 }
@@ -1173,6 +1175,7 @@ typedef struct {
   int* return_code;
   double* seconds;     // [2]: warmup, sampling
   unsigned long long* draws_used;  // [2]: uniforms, normals
+  long long* n_grad_total;
 } oracle_chain_out;
 
 // Runs num_chains chains (chain ids init_chain_id + i) on num_threads host
@@ -1233,6 +1236,7 @@ int oracle_sample(void* mp, const oracle_sampler_config* c, int num_chains,
         dst.draws_used[0] = o.n_uniform;
         dst.draws_used[1] = o.n_normal;
       }
+      if (dst.n_grad_total) *dst.n_grad_total = o.n_grad_total;
     }
   };
   int nt = std::max(1, std::min(num_threads, num_chains));

@@ -31,6 +31,11 @@ const std::string& last_error() { return g_last_error; }
 
 using namespace gbn;
 
+static int fail(int code, const std::string& msg) {
+  set_last_error(msg);
+  return code;
+}
+
 struct gbnuts_model {
   ModelDesc desc;
   void* d_X = nullptr;
@@ -44,11 +49,38 @@ struct gbnuts_model {
   double* d_grad = nullptr;
   int scratch_C = 0;
   cudaStream_t stream = nullptr;
+  void* d_tc_xt = nullptr;
+  float* d_tc_yt = nullptr;
 };
 
-static int fail(int code, const std::string& msg) {
-  set_last_error(msg);
-  return code;
+// Builds the tensor-core tiles of X on first use of the bf16x3 form.
+static int ensure_precision(gbnuts_model* m, int precision) {
+  if (precision < GBNUTS_PREC_FP64 || precision > GBNUTS_PREC_BF16X3)
+    return fail(GBNUTS_USAGE, "unknown precision");
+  if (precision != GBNUTS_PREC_BF16X3) return GBNUTS_OK;
+  if (!tc_supported(m->desc))
+    return fail(GBNUTS_USAGE,
+                "bf16x3 precision needs a logistic or Poisson GLM with K + intercept <= 128");
+  if (m->d_tc_xt) return GBNUTS_OK;
+  int tiles = 0;
+  int rc = tc_prepare(m->desc, &m->d_tc_xt, &m->d_tc_yt, &tiles, m->stream);
+  if (rc) return rc;
+  GBN_CUDA_TRY(cudaStreamSynchronize(m->stream));
+  m->desc.tc_xt = m->d_tc_xt;
+  m->desc.tc_yt = m->d_tc_yt;
+  m->desc.tc_tiles = tiles;
+  return GBNUTS_OK;
+}
+
+static int check_device_error(GradWorkspace& ws) {
+  if (!ws.err) return GBNUTS_OK;
+  int e = 0;
+  GBN_CUDA_TRY(cudaMemcpy(&e, ws.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    cudaMemset(ws.err, 0, sizeof(int));
+    return fail(GBNUTS_SOFTWARE, "a device wait timed out (code " + std::to_string(e) + ")");
+  }
+  return GBNUTS_OK;
 }
 
 static void host_names(const ModelDesc& m, bool constrained_unused, std::vector<std::string>& out) {
@@ -233,6 +265,8 @@ int gbnuts_model_create(int kind, const void* X, int x_dtype, const double* y,
 void gbnuts_model_destroy(gbnuts_model* m) {
   if (!m) return;
   free_workspace(m->ws);
+  if (m->d_tc_xt) cudaFree(m->d_tc_xt);
+  if (m->d_tc_yt) cudaFree(m->d_tc_yt);
   if (m->d_theta) cudaFree(m->d_theta);
   if (m->d_X) cudaFree(m->d_X);
   if (m->d_y) cudaFree(m->d_y);
@@ -259,7 +293,9 @@ static int eval_points(gbnuts_model* m, int C, const double* theta, int propto, 
                        double* lp, double* grad, int precision) {
   if (!m || C <= 0 || !theta) return fail(GBNUTS_USAGE, "bad arguments");
   const int D = m->desc.D;
-  int rc = ensure_scratch(m, C);
+  int rc = ensure_precision(m, precision);
+  if (rc) return rc;
+  rc = ensure_scratch(m, C);
   if (rc) return rc;
   rc = prepare_workspace(m->desc, m->h_group_off.data(), C, precision, m->ws);
   if (rc) return rc;
@@ -274,7 +310,7 @@ static int eval_points(gbnuts_model* m, int C, const double* theta, int propto, 
     GBN_CUDA_TRY(cudaMemcpyAsync(grad, m->d_grad, (size_t)C * D * sizeof(double),
                                  cudaMemcpyDeviceToHost, m->stream));
   GBN_CUDA_TRY(cudaStreamSynchronize(m->stream));
-  return GBNUTS_OK;
+  return check_device_error(m->ws);
 }
 
 int gbnuts_log_prob(gbnuts_model* m, const double* theta, int propto, int jacobian,
@@ -299,7 +335,9 @@ int gbnuts_log_prob_grad_batch_device(gbnuts_model* m, int C, const double* d_th
                                       double* d_lp, double* d_grad, int precision,
                                       void* stream) {
   if (!m || C <= 0 || !d_theta || !d_lp || !d_grad) return fail(GBNUTS_USAGE, "bad arguments");
-  int rc = prepare_workspace(m->desc, m->h_group_off.data(), C, precision, m->ws);
+  int rc = ensure_precision(m, precision);
+  if (rc) return rc;
+  rc = prepare_workspace(m->desc, m->h_group_off.data(), C, precision, m->ws);
   if (rc) return rc;
   return launch_log_prob_grad(m->desc, precision, d_theta, m->desc.D, C, nullptr, d_lp, d_grad,
                               m->desc.D, 1, 1, m->ws, static_cast<cudaStream_t>(stream),
@@ -488,7 +526,9 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   GBN_CUDA_TRY(cudaMemsetAsync(d_abort, 0, sizeof(int), st));
   GBN_CUDA_TRY(cudaMemsetAsync(d_grad, 0, (size_t)C * cfg.ld * sizeof(double), st));
   GBN_CUDA_TRY(cudaMemsetAsync(d_draws, 0, (size_t)C * out->max_rows * n_cols * sizeof(double), st));
-  int prc = prepare_workspace(m->desc, m->h_group_off.data(), C, rc->precision, m->ws);
+  int prc = ensure_precision(m, rc->precision);
+  if (prc) return prc;
+  prc = prepare_workspace(m->desc, m->h_group_off.data(), C, rc->precision, m->ws);
   if (prc) return prc;
 
   int* h_done = nullptr;
@@ -594,6 +634,7 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
       out->seconds[2 * c + 1] = wall_s * (1.0 - frac);
     }
   }
+  if (status_rc == GBNUTS_OK) status_rc = check_device_error(m->ws);
   out->total_ms = total_ms;
   out->grad_ms = grad_n ? grad_ms_sum / grad_n : 0.0;
   out->steps = step;

@@ -44,6 +44,10 @@ struct ModelDesc {
   const int* group;  // N (hierarchical) or nullptr
   double s_base, s_tau, s_sigma, s_beta;  // prior scales
   double sum_lgamma_y;                    // Poisson constant, for propto = false
+  // tensor-core form: X pre-tiled as bf16 hi/lo (128-row tiles), y per tile row
+  const void* tc_xt;
+  const float* tc_yt;
+  int tc_tiles;
 };
 
 // Number of per-(split, chain) partial sums: lp, sum r, sum r z_g, sum e^2, beta[K].
@@ -55,6 +59,8 @@ struct GradWorkspace {
   double* partial = nullptr;   // [S][C][NP]
   double* gz = nullptr;        // [C][J] raw group sums (hierarchical)
   long long* split_rows = nullptr;  // [S+1] device
+  int* err = nullptr;               // device error flag of bounded waits
+  int precision = -1;
   std::vector<long long> h_split_rows;
   size_t bytes = 0;
 };
@@ -75,5 +81,17 @@ int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int
 // Maximum chains per block of the partial kernel for a given K (0 if K is
 // beyond what the kernel supports).
 int chains_per_block(int K);
+
+// Tensor-core (bf16 hi/lo) GLM path.
+int tc_max_features();
+int tc_splits(const ModelDesc& m, int C);
+int tc_prepare(const ModelDesc& m, void** xt, float** yt, int* n_tiles, cudaStream_t st);
+int launch_tc(const ModelDesc& m, const double* Q, int ldq, int C, const int* active,
+              GradWorkspace& ws, cudaStream_t st);
+// Whether the model can use the tensor-core form.
+inline bool tc_supported(const ModelDesc& m) {
+  return (m.link == LINK_LOGIT || m.link == LINK_POISSON_LOG) && m.off_z < 0 &&
+         m.K + m.has_base <= 128;
+}
 
 }  // namespace gbn

@@ -415,27 +415,37 @@ static void dispatch_x(const ModelDesc& m, const double* Q, int ldq, int C,
 
 int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int precision,
                       GradWorkspace& ws) {
-  (void)precision;
   const int CB = chains_per_block(m.K);
   if (CB == 0) {
     set_last_error("K beyond the supported maximum (2048)");
     return GBNUTS_USAGE;
   }
-  const int chain_blocks = (C + CB - 1) / CB;
-  // Splits: enough CTAs for ~2 waves over 152 SMs, at least 64 rows each.
-  long long max_s = std::max(1LL, m.N / 64);
-  int S = (int)std::min<long long>(max_s, std::max(1, (2 * 152 + chain_blocks - 1) / chain_blocks));
-  if (m.off_z >= 0) S = std::min(S, m.J);
-  S = std::max(S, 1);
+  int S;
+  if (precision == GBNUTS_PREC_BF16X3) {
+    if (!tc_supported(m)) {
+      set_last_error("bf16x3 precision needs a logistic or Poisson GLM with K + intercept <= 128");
+      return GBNUTS_USAGE;
+    }
+    S = tc_splits(m, C);
+  } else {
+    const int chain_blocks = (C + CB - 1) / CB;
+    // Splits: enough CTAs for ~2 waves over 152 SMs, at least 64 rows each.
+    long long max_s = std::max(1LL, m.N / 64);
+    S = (int)std::min<long long>(max_s, std::max(1, (2 * 152 + chain_blocks - 1) / chain_blocks));
+    if (m.off_z >= 0) S = std::min(S, m.J);
+    S = std::max(S, 1);
+  }
   const int NP = n_partials(m);
   size_t need = (size_t)S * C * NP * sizeof(double) +
                 (m.off_z >= 0 ? (size_t)C * m.J * sizeof(double) : 0) +
-                (size_t)(S + 1) * sizeof(long long);
-  if (ws.C == C && ws.S == S && ws.NP == NP && ws.partial) return GBNUTS_OK;
+                (size_t)(S + 1) * sizeof(long long) + 16;
+  if (ws.C == C && ws.S == S && ws.NP == NP && ws.partial && ws.precision == precision)
+    return GBNUTS_OK;
   free_workspace(ws);
   ws.C = C;
   ws.S = S;
   ws.NP = NP;
+  ws.precision = precision;
   ws.h_split_rows.assign(S + 1, 0);
   for (int s = 0; s <= S; ++s) {
     if (m.off_z >= 0) {
@@ -455,8 +465,11 @@ int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int pre
     off += (size_t)C * m.J * sizeof(double);
   }
   ws.split_rows = reinterpret_cast<long long*>(base + off);
+  off += (size_t)(S + 1) * sizeof(long long);
+  ws.err = reinterpret_cast<int*>(base + off);
   GBN_CUDA_TRY(cudaMemcpy(ws.split_rows, ws.h_split_rows.data(),
                           (S + 1) * sizeof(long long), cudaMemcpyHostToDevice));
+  GBN_CUDA_TRY(cudaMemset(ws.err, 0, sizeof(int)));
   return GBNUTS_OK;
 }
 
@@ -476,6 +489,9 @@ int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int
     dispatch_x<double>(m, Q, ldq, C, active, ws, stream);
   } else if (precision == GBNUTS_PREC_FP32) {
     dispatch_x<float>(m, Q, ldq, C, active, ws, stream);
+  } else if (precision == GBNUTS_PREC_BF16X3 && m.tc_xt != nullptr) {
+    int rc = launch_tc(m, Q, ldq, C, active, ws, stream);
+    if (rc) return rc;
   } else {
     set_last_error("precision not available for this model");
     return GBNUTS_USAGE;

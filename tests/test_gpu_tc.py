@@ -1,0 +1,92 @@
+"""Tensor-core (tcgen05, bf16 hi/lo) gradient path.
+
+The probe pushes small-integer bf16 matrices through both contraction layouts
+the gradient uses (K-major X.Theta^T and MN-major X^T.R); with such inputs the
+fp32 results are exact, so they must equal NumPy's.  The bf16x3 gradient is
+then checked against the FP64 oracle: lp within 1e-5 relative, gradient
+within 1e-4 relative in the 2-norm.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests.datasets import make_dataset
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16_bits(a):
+    return (np.ascontiguousarray(a, dtype=np.float32).view(np.uint32) >> 16).astype(np.uint16)
+
+
+def test_descriptor_probe_exact():
+    from stan_gb300 import _lib
+    lib = _lib.load()
+    f = lib.gbnuts_tc_probe
+    u16 = ctypes.POINTER(ctypes.c_uint16)
+    fp = ctypes.POINTER(ctypes.c_float)
+    f.restype = ctypes.c_int
+    f.argtypes = [u16, u16, u16, fp, fp]
+    rng = np.random.default_rng(0)
+    A = rng.integers(-2, 3, size=(128, 128)).astype(np.float32)
+    B = rng.integers(-2, 3, size=(64, 128)).astype(np.float32)
+    R = rng.integers(-2, 3, size=(128, 64)).astype(np.float32)
+    a, b, r = _bf16_bits(A), _bf16_bits(B), _bf16_bits(R)
+    D1 = np.zeros((128, 64), dtype=np.float32)
+    D2 = np.zeros((128, 64), dtype=np.float32)
+    rc = f(a.ctypes.data_as(u16), b.ctypes.data_as(u16), r.ctypes.data_as(u16),
+           D1.ctypes.data_as(fp), D2.ctypes.data_as(fp))
+    assert rc == 0, _lib.last_error()
+    assert np.array_equal(D1, A @ B.T), "K-major contraction (X . Theta^T) differs"
+    assert np.array_equal(D2, A.T @ R), "MN-major contraction (X^T . R) differs"
+
+
+@pytest.mark.parametrize("kind", ["logistic", "logistic_100k", "poisson"])
+def test_bf16x3_gradient_matches_fp64_oracle(kind):
+    from stan_gb300 import Model
+    ds = make_dataset(kind, small=True, seed=9)
+    m = Model.from_dataset(ds)
+    om = ds.oracle_model()
+    C = 70  # two chain groups, the second partly empty
+    th = np.random.default_rng(4).normal(size=(C, m.D)) * 0.3
+    lp, g = m.log_prob_grad_batch(th, "bf16x3")
+    for c in range(C):
+        lpo, go = om.log_prob_grad(th[c])
+        assert abs(lp[c] - lpo) <= 1e-5 * abs(lpo), (c, lp[c], lpo)
+        assert np.linalg.norm(g[c] - go) <= 1e-4 * np.linalg.norm(go), c
+
+
+def test_bf16x3_full_size_logistic():
+    """N = 100000, K = 100 at 1024 chains (the benchmark shape)."""
+    from stan_gb300 import Model
+    ds = make_dataset("logistic_100k", small=False, seed=1)
+    m = Model.from_dataset(ds)
+    om = ds.oracle_model()
+    C = 1024
+    th = np.random.default_rng(5).normal(size=(C, m.D)) * 0.05
+    lp, g = m.log_prob_grad_batch(th, "bf16x3")
+    lp64, g64 = m.log_prob_grad_batch(th, "fp64")
+    for c in (0, 1, 63, 64, 511, 1023):
+        lpo, go = om.log_prob_grad(th[c])
+        assert abs(lp64[c] - lpo) <= 1e-12 * abs(lpo)
+        assert abs(lp[c] - lpo) <= 1e-5 * abs(lpo)
+        assert np.linalg.norm(g[c] - go) <= 1e-4 * np.linalg.norm(go)
+    rel = np.linalg.norm(g - g64, axis=1) / np.linalg.norm(g64, axis=1)
+    assert rel.max() <= 1e-4
+
+
+def test_bf16x3_posterior_matches_fp64_within_mcse():
+    """Mixed-precision sampling gives the FP64 posterior: means within 4 MCSE."""
+    from stan_gb300 import Model, analyze, sampler
+    ds = make_dataset("logistic", small=False, seed=2)   # N = 1000, K = 25
+    m = Model.from_dataset(ds)
+    kw = dict(num_chains=8, num_warmup=500, num_samples=1000, random_seed=3)
+    r64 = sampler.run(m, precision="fp64", **kw)
+    rmx = sampler.run(m, precision="bf16x3", **kw)
+    assert np.all(r64.status == 0) and np.all(rmx.status == 0)
+    d64 = r64.sampling_draws()[:, :, 7:]
+    dmx = rmx.sampling_draws()[:, :, 7:]
+    for j in range(m.D):
+        se = np.hypot(analyze.mcse_mean(d64[:, :, j]), analyze.mcse_mean(dmx[:, :, j]))
+        assert abs(d64[:, :, j].mean() - dmx[:, :, j].mean()) <= 4 * se, j
