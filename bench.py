@@ -204,7 +204,9 @@ def run_ours(args, ws, rank, local):
     else:
         bound, peak, unit, ach = "tensor", peaks.get("bf16_tflops", 1900.0), "TFLOP/s", flops / (mean_ms * 1e-3) / 1e12
     roof = {"bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
-            "traffic": None, "kernel": "loglik_partial_kernel", "mean_launch_ms": mean_ms,
+            "traffic": None,
+            "kernel": "glm_tc_kernel" if args.precision == "bf16x3" else "loglik_partial_kernel",
+            "mean_launch_ms": mean_ms,
             "flops_per_launch": flops}
     out = {"metric": "grad evals/s", "value": value, "unit": "grad evals/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup,
@@ -283,6 +285,25 @@ def run_reference(args, ws, rank):
                     "d2h_bytes_per_step": 0}}
 
 
+def profile_case(args):
+    """Small, self-terminating invocations of the workload's kernels, for ncu."""
+    from stan_gb300 import Model, _lib, sampler, workloads
+    wl = WORKLOADS[args.workload]
+    ds = workloads.make_dataset(wl["kind"], seed=1)
+    _lib.load(build_if_missing=False)
+    model = Model.from_dataset(ds)
+    C = wl["chains"]
+    if args.case == "grad":
+        th = np.random.default_rng(0).normal(size=(C, model.D)) * 0.05
+        for _ in range(2):
+            lp, _g = model.log_prob_grad_batch(th, args.precision)
+        print(json.dumps({"case": "grad", "chains": C, "lp0": float(lp[0])}))
+    else:
+        r = sampler.run(model, num_chains=C, num_warmup=args.short_iters, num_samples=0,
+                        precision=args.precision, random_seed=1)
+        print(json.dumps({"case": "shortfit", "steps": int(r.steps), "ms": r.total_ms}))
+
+
 _dist = None
 
 
@@ -329,12 +350,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="logistic_100k", choices=list(WORKLOADS))
-    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "bf16x3"])
+    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "fp32", "bf16x3"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--case", default="fit", choices=["fit", "grad", "shortfit"],
+                    help="fit: the benchmark; grad: two batched-gradient launches of the "
+                         "workload (for kernel captures); shortfit: a fit of --short-iters "
+                         "warmup iterations (for launch lists)")
+    ap.add_argument("--short-iters", type=int, default=40)
     args = ap.parse_args()
+    if args.case != "fit":
+        profile_case(args)
+        return
     ws, rank, local = dist_env()
     if args.impl == "reference":
         if rank != 0:

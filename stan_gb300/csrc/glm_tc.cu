@@ -32,13 +32,21 @@ constexpr int NC = 64;    // chains per CTA
 constexpr int TILE_BYTES = TM * TK * 2;      // one bf16 part of an X tile
 constexpr int THETA_BYTES = NC * TK * 2;     // one bf16 part of Theta
 constexpr int R_BYTES = NC * TM * 2;         // one bf16 part of R
+constexpr int NUM_EPI_WARPS = 8;             // two per TMEM lane quarter (32 columns each)
+constexpr int TC_THREADS = 64 + 32 * NUM_EPI_WARPS;
+// pipelined kernel: two X stages (hi + lo each), Theta, R, lp scratch, barriers
+constexpr int Y_BYTES = TM * 4;               // y of one tile (fp32)
+constexpr int STAGE_BYTES = 2 * TILE_BYTES + 1024;  // X hi, X lo, y (padded)
 constexpr int SMEM_X = 0;
-constexpr int SMEM_T = SMEM_X + 2 * TILE_BYTES;
+constexpr int SMEM_T = SMEM_X + 2 * STAGE_BYTES;
 constexpr int SMEM_R = SMEM_T + 2 * THETA_BYTES;
 constexpr int SMEM_LP = SMEM_R + 2 * R_BYTES;
-constexpr int SMEM_BAR = SMEM_LP + 4 * NC * 4;
-constexpr int SMEM_TOTAL = SMEM_BAR + 64;
+constexpr int SMEM_BAR = SMEM_LP + 4 * NC * 8;  // lp partials [quarter][chain]
+constexpr int SMEM_TOTAL = SMEM_BAR + 256;
 constexpr int SMEM_ALLOC = SMEM_TOTAL + 1024;  // slack for 1 KiB alignment
+// barrier slots (uint64 each) inside SMEM_BAR
+enum { B_XFULL = 0, B_XEMPTY = 2, B_D1FULL = 4, B_D1EMPTY = 6, B_RFULL = 8, B_REMPTY = 9,
+       B_D2FULL = 10, B_COUNT = 11 };
 
 int tc_max_features() { return TK; }
 
@@ -89,72 +97,68 @@ struct TcArgs {
   int* err;
 };
 
-// Warp transpose reduction: v[64] per lane (one row each) -> lane l holds the
-// sums over the warp's 32 rows of chains 2l and 2l+1.
-__device__ __forceinline__ void warp_reduce_scatter64(float (&v)[64], float& s0, float& s1) {
+// Warp transpose reduction: v[32] per lane (one row each) -> returns, in lane
+// l, the sum over the warp's 32 rows of column l.
+__device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32]) {
   const int lane = threadIdx.x & 31;
-  float w[32];
+  float w[16];
   {
     const bool up = lane & 16;
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      float send = up ? v[i] : v[32 + i];
-      float keep = up ? v[32 + i] : v[i];
+    for (int i = 0; i < 16; ++i) {
+      float send = up ? v[i] : v[16 + i];
+      float keep = up ? v[16 + i] : v[i];
       w[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
     }
   }
-  float x[16];
+  float x[8];
   {
     const bool up = lane & 8;
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      float send = up ? w[i] : w[16 + i];
-      float keep = up ? w[16 + i] : w[i];
+    for (int i = 0; i < 8; ++i) {
+      float send = up ? w[i] : w[8 + i];
+      float keep = up ? w[8 + i] : w[i];
       x[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
     }
   }
-  float y[8];
+  float y[4];
   {
     const bool up = lane & 4;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      float send = up ? x[i] : x[8 + i];
-      float keep = up ? x[8 + i] : x[i];
+    for (int i = 0; i < 4; ++i) {
+      float send = up ? x[i] : x[4 + i];
+      float keep = up ? x[4 + i] : x[i];
       y[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
     }
   }
-  float z[4];
+  float z[2];
   {
     const bool up = lane & 2;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      float send = up ? y[i] : y[4 + i];
-      float keep = up ? y[4 + i] : y[i];
+    for (int i = 0; i < 2; ++i) {
+      float send = up ? y[i] : y[2 + i];
+      float keep = up ? y[2 + i] : y[i];
       z[i] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
     }
   }
-  {
-    const bool up = lane & 1;
-    float send0 = up ? z[0] : z[2], keep0 = up ? z[2] : z[0];
-    float send1 = up ? z[1] : z[3], keep1 = up ? z[3] : z[1];
-    s0 = keep0 + __shfl_xor_sync(0xffffffffu, send0, 1);
-    s1 = keep1 + __shfl_xor_sync(0xffffffffu, send1, 1);
-  }
+  const bool up = lane & 1;
+  float send = up ? z[0] : z[1], keep = up ? z[1] : z[0];
+  return keep + __shfl_xor_sync(0xffffffffu, send, 1);
 }
 
-__global__ void __launch_bounds__(128, 1) glm_tc_kernel(TcArgs a) {
+template <int LINK, bool XLO>
+__global__ void __launch_bounds__(TC_THREADS, 1) glm_tc_kernel(TcArgs a) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  unsigned char* sXh = sm + SMEM_X;
-  unsigned char* sXl = sXh + TILE_BYTES;
   unsigned char* sTh = sm + SMEM_T;
   unsigned char* sTl = sTh + THETA_BYTES;
   unsigned char* sRh = sm + SMEM_R;
   unsigned char* sRl = sRh + R_BYTES;
-  float* sLP = reinterpret_cast<float*>(sm + SMEM_LP);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + SMEM_BAR);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + SMEM_BAR + 16);
+  double* sLP = reinterpret_cast<double*>(sm + SMEM_LP);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + SMEM_BAR);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + SMEM_BAR + 8 * B_COUNT);
+  volatile int* abort_s = reinterpret_cast<volatile int*>(sm + SMEM_BAR + 8 * B_COUNT + 8);
   __shared__ int act_s[NC];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -182,168 +186,215 @@ __global__ void __launch_bounds__(128, 1) glm_tc_kernel(TcArgs a) {
     *reinterpret_cast<__nv_bfloat16*>(sTl + off) = lo;
   }
   if (tid == 0) {
-    mbar_init(bar, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&bars[B_XFULL + b], 1);
+      mbar_init(&bars[B_XEMPTY + b], 1);
+      mbar_init(&bars[B_D1FULL + b], 1);
+      mbar_init(&bars[B_D1EMPTY + b], NUM_EPI_WARPS);
+    }
+    mbar_init(&bars[B_RFULL], NUM_EPI_WARPS);
+    mbar_init(&bars[B_REMPTY], 1);
+    mbar_init(&bars[B_D2FULL], 1);
+    *abort_s = 0;
     fence_mbar_init();
   }
-  if (warp == 0) tmem_alloc(tmem_slot, 128);
+  if (warp == 0) tmem_alloc(tmem_slot, 256);
+  fence_proxy_async();
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t tD1 = tmem;        // columns 0..63
-  const uint32_t tD2 = tmem + 64;   // columns 64..127
+  const uint32_t tD2 = tmem + 128;
 
   const int t_begin = (int)((long long)a.n_tiles * s / a.S);
   const int t_end = (int)((long long)a.n_tiles * (s + 1) / a.S);
-  const uint32_t idesc1 = make_idesc_bf16(TM, NC, 0, 0);
-  const uint32_t idesc2 = make_idesc_bf16(TK, NC, 1, 1);
-  const uint32_t aXh = smem_u32(sXh), aXl = smem_u32(sXl);
-  const uint32_t aTh = smem_u32(sTh), aTl = smem_u32(sTl);
-  const uint32_t aRh = smem_u32(sRh), aRl = smem_u32(sRl);
-  uint32_t phase = 0;
-  bool ok = true;
-  double lp_acc = 0.0;
+  const int n = t_end - t_begin;
+  const uint32_t x_bytes = XLO ? 2u * TILE_BYTES : (uint32_t)TILE_BYTES;
 
-  for (int t = t_begin; t < t_end && ok; ++t) {
-    // X tile (hi, lo): 2 x 32 KiB contiguous
-    {
-      const uint4* src_h = reinterpret_cast<const uint4*>(a.xt + (size_t)(2 * t) * (TM * TK));
-      const uint4* src_l = reinterpret_cast<const uint4*>(a.xt + (size_t)(2 * t + 1) * (TM * TK));
-      uint4* dh = reinterpret_cast<uint4*>(sXh);
-      uint4* dl = reinterpret_cast<uint4*>(sXl);
-      for (int i = tid; i < TILE_BYTES / 16; i += blockDim.x) {
-        dh[i] = src_h[i];
-        if (a.x_has_lo) dl[i] = src_l[i];
-      }
-    }
-    fence_proxy_async();
-    __syncthreads();
-    // GEMM1: eta = X . Theta^T
-    if (tid == 0) {
-      fence_after_sync();
-#pragma unroll 1
-      for (int ks = 0; ks < TK / 16; ++ks) {
-        const uint64_t ah = make_desc(aXh + 256 * ks, 128, (TK / 8) * 128);
-        const uint64_t al = make_desc(aXl + 256 * ks, 128, (TK / 8) * 128);
-        const uint64_t bh = make_desc(aTh + 256 * ks, 128, (TK / 8) * 128);
-        const uint64_t bl = make_desc(aTl + 256 * ks, 128, (TK / 8) * 128);
-        mma_bf16(tD1, ah, bh, idesc1, ks > 0 ? 1u : 0u);
-        mma_bf16(tD1, ah, bl, idesc1, 1u);
-        if (a.x_has_lo) mma_bf16(tD1, al, bh, idesc1, 1u);
-      }
-      mma_commit(bar);
-    }
-    ok = mbar_wait(bar, phase, a.err, 1);
-    phase ^= 1u;
-    fence_after_sync();
-    // link on the eta tile: this thread's row, 64 chains
-    {
-      const int r = warp * 32 + lane;
-      const long long row = (long long)t * TM + r;
-      const bool valid = row < a.N;
-      const float yv = a.yt[(size_t)t * TM + r];
-      float v[64];
-      tmem_ld32(tD1 + ((uint32_t)(warp * 32) << 16), v);
-      tmem_ld32(tD1 + ((uint32_t)(warp * 32) << 16) + 32, v + 32);
-      tmem_ld_wait();
-#pragma unroll
-      for (int g = 0; g < NC / 8; ++g) {
-        __align__(16) __nv_bfloat16 hi8[8], lo8[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int c = g * 8 + j;
-          const float eta = v[c];
-          float term, resid;
-          if (a.link == LINK_LOGIT) {
-            const float e = __expf(-fabsf(eta));
-            const float d = 1.f + e;
-            const float inv = __fdividef(1.f, d);
-            const float sig = eta >= 0.f ? inv : e * inv;
-            term = yv * eta - (fmaxf(eta, 0.f) + __logf(d));
-            resid = yv - sig;
-          } else {
-            const float mu = __expf(eta);
-            term = yv * eta - mu;
-            resid = yv - mu;
-          }
-          if (!valid) {
-            term = 0.f;
-            resid = 0.f;
-          }
-          v[c] = term;
-          split_bf16(resid, hi8[j], lo8[j]);
+  if (n > 0) {
+    if (warp == 0) {
+      // ---- producer: X tiles through the 2-stage ring
+      if (lane == 0) {
+        for (int i = 0; i < n; ++i) {
+          const int b = i & 1, u = i >> 1;
+          if (!mbar_wait_abortable(&bars[B_XEMPTY + b], (u & 1) ^ 1, abort_s, a.err, 11)) break;
+          unsigned char* dst = sm + SMEM_X + b * STAGE_BYTES;
+          const __nv_bfloat16* src = a.xt + (size_t)(2 * (t_begin + i)) * (TM * TK);
+          mbar_arrive_expect_tx(&bars[B_XFULL + b], x_bytes + Y_BYTES);
+          bulk_copy_g2s(dst, src, TILE_BYTES, &bars[B_XFULL + b]);
+          if (XLO)
+            bulk_copy_g2s(dst + TILE_BYTES, src + TM * TK, TILE_BYTES, &bars[B_XFULL + b]);
+          bulk_copy_g2s(dst + 2 * TILE_BYTES, a.yt + (size_t)(t_begin + i) * TM, Y_BYTES,
+                        &bars[B_XFULL + b]);
         }
-        const uint32_t off = (uint32_t)(g * ((TM / 8) * 128) + (r >> 3) * 128 + (r & 7) * 16);
-        *reinterpret_cast<uint4*>(sRh + off) = *reinterpret_cast<const uint4*>(hi8);
-        *reinterpret_cast<uint4*>(sRl + off) = *reinterpret_cast<const uint4*>(lo8);
       }
-      float s0, s1;
-      warp_reduce_scatter64(v, s0, s1);
-      sLP[warp * NC + 2 * lane] = s0;
-      sLP[warp * NC + 2 * lane + 1] = s1;
-    }
-    fence_before_sync();
-    fence_proxy_async();
-    __syncthreads();
-    if (tid < NC)
-      lp_acc += (double)sLP[tid] + (double)sLP[NC + tid] + (double)sLP[2 * NC + tid] +
-                (double)sLP[3 * NC + tid];
-    // GEMM2: G += X^T . R  (both operands MN-major)
-    if (tid == 0) {
-      fence_after_sync();
+      __syncwarp();
+    } else if (warp == 1) {
+      // ---- MMA issuer: GEMM1 of tile i, then GEMM2 of tile i-1
+      if (lane == 0) {
+        const uint32_t idesc1 = make_idesc_bf16(TM, NC, 0, 0);
+        const uint32_t idesc2 = make_idesc_bf16(TK, NC, 1, 1);
+        const uint32_t aTh = smem_u32(sTh), aTl = smem_u32(sTl);
+        const uint32_t aRh = smem_u32(sRh), aRl = smem_u32(sRl);
+        bool ok = true;
+        auto gemm2 = [&](int j) -> bool {
+          if (!mbar_wait_abortable(&bars[B_RFULL], j & 1, abort_s, a.err, 13)) return false;
+          fence_after_sync();
+          const uint32_t aXh = smem_u32(sm + SMEM_X + (j & 1) * STAGE_BYTES);
+          const uint32_t aXl = aXh + TILE_BYTES;
 #pragma unroll 1
-      for (int ks = 0; ks < TM / 16; ++ks) {
-        const uint64_t ah = make_desc(aXh + 4096 * ks, (TM / 8) * 128 * 1, 128);
-        const uint64_t al = make_desc(aXl + 4096 * ks, (TM / 8) * 128 * 1, 128);
-        const uint64_t bh = make_desc(aRh + 256 * ks, 128, (TM / 8) * 128);
-        const uint64_t bl = make_desc(aRl + 256 * ks, 128, (TM / 8) * 128);
-        const uint32_t acc0 = (t > t_begin || ks > 0) ? 1u : 0u;
-        mma_bf16(tD2, ah, bh, idesc2, acc0);
-        mma_bf16(tD2, ah, bl, idesc2, 1u);
-        if (a.x_has_lo) mma_bf16(tD2, al, bh, idesc2, 1u);
+          for (int ks = 0; ks < TM / 16; ++ks) {
+            const uint64_t ah = make_desc(aXh + 4096 * ks, (TM / 8) * 128, 128);
+            const uint64_t al = make_desc(aXl + 4096 * ks, (TM / 8) * 128, 128);
+            const uint64_t bh = make_desc(aRh + 256 * ks, 128, (TM / 8) * 128);
+            const uint64_t bl = make_desc(aRl + 256 * ks, 128, (TM / 8) * 128);
+            const uint32_t acc0 = (j > 0 || ks > 0) ? 1u : 0u;
+            mma_bf16(tD2, ah, bh, idesc2, acc0);
+            mma_bf16(tD2, ah, bl, idesc2, 1u);
+            if (XLO) mma_bf16(tD2, al, bh, idesc2, 1u);
+          }
+          mma_commit(&bars[B_REMPTY]);
+          mma_commit(&bars[B_XEMPTY + (j & 1)]);
+          return true;
+        };
+        for (int i = 0; i < n && ok; ++i) {
+          const int b = i & 1, u = i >> 1;
+          ok = mbar_wait_abortable(&bars[B_XFULL + b], u & 1, abort_s, a.err, 12) &&
+               mbar_wait_abortable(&bars[B_D1EMPTY + b], (u & 1) ^ 1, abort_s, a.err, 14);
+          if (!ok) break;
+          fence_after_sync();
+          const uint32_t aXh = smem_u32(sm + SMEM_X + b * STAGE_BYTES);
+          const uint32_t aXl = aXh + TILE_BYTES;
+          const uint32_t tD1 = tmem + 64 * b;
+#pragma unroll 1
+          for (int ks = 0; ks < TK / 16; ++ks) {
+            const uint64_t ah = make_desc(aXh + 256 * ks, 128, (TK / 8) * 128);
+            const uint64_t al = make_desc(aXl + 256 * ks, 128, (TK / 8) * 128);
+            const uint64_t bh = make_desc(aTh + 256 * ks, 128, (TK / 8) * 128);
+            const uint64_t bl = make_desc(aTl + 256 * ks, 128, (TK / 8) * 128);
+            mma_bf16(tD1, ah, bh, idesc1, ks > 0 ? 1u : 0u);
+            mma_bf16(tD1, ah, bl, idesc1, 1u);
+            if (XLO) mma_bf16(tD1, al, bh, idesc1, 1u);
+          }
+          mma_commit(&bars[B_D1FULL + b]);
+          if (i > 0) ok = gemm2(i - 1);
+        }
+        if (ok) ok = gemm2(n - 1);
+        mma_commit(&bars[B_D2FULL]);
       }
-      mma_commit(bar);
-    }
-    ok = mbar_wait(bar, phase, a.err, 2) && ok;
-    phase ^= 1u;
-    fence_after_sync();
-  }
-  __syncthreads();
-  // gradient partials: this thread's feature row of G, 64 chains
-  {
-    const int k = warp * 32 + lane;
-    float g[64];
-    const bool have = ok && (t_end > t_begin);
-    if (have) {
-      tmem_ld32(tD2 + ((uint32_t)(warp * 32) << 16), g);
-      tmem_ld32(tD2 + ((uint32_t)(warp * 32) << 16) + 32, g + 32);
-      tmem_ld_wait();
+      __syncwarp();
     } else {
+      // ---- epilogue: link on eta, R to shared memory, lp partial sums.
+      // Warp w (2..9): TMEM lane quarter q = w % 4 (rows 32q..32q+31),
+      // chain half h (columns 32h..32h+31).
+      const int q = warp & 3;
+      const int h = (warp - 2) >> 2;
+      const int r = q * 32 + lane;
+      double lp_acc = 0.0;
+      bool ok = true;
+      for (int i = 0; i < n && ok; ++i) {
+        const int b = i & 1, u = i >> 1;
+        const int t = t_begin + i;
+        if (!warp_wait(&bars[B_D1FULL + b], u & 1, abort_s, a.err, 15)) {
+          ok = false;
+          break;
+        }
+        fence_after_sync();
+        float v[32];
+        tmem_ld32(tmem + 64 * b + 32 * h + ((uint32_t)(q * 32) << 16), v);
+        tmem_ld_wait();
+        fence_before_sync();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bars[B_D1EMPTY + b]);
+        const long long row = (long long)t * TM + r;
+        const bool valid = row < a.N;
+        const float yv =
+            reinterpret_cast<const float*>(sm + SMEM_X + b * STAGE_BYTES + 2 * TILE_BYTES)[r];
+        uint32_t rh[16], rl[16];
 #pragma unroll
-      for (int c = 0; c < 64; ++c) g[c] = 0.f;
-    }
-    int slot = -1;
-    if (k < hb)
-      slot = 1;
-    else if (k - hb < a.K)
-      slot = 4 + (k - hb);
-    if (slot >= 0) {
+        for (int c = 0; c < 32; c += 2) {
+          float res[2];
 #pragma unroll
-      for (int c = 0; c < NC; ++c)
-        if (act_s[c]) a.P[((size_t)s * a.C + c0 + c) * a.NP + slot] = (double)g[c];
-    }
-    if (tid < NC && act_s[tid]) {
-      double* dst = a.P + ((size_t)s * a.C + c0 + tid) * a.NP;
-      dst[0] = lp_acc;
-      dst[2] = 0.0;
-      dst[3] = 0.0;
+          for (int j = 0; j < 2; ++j) {
+            const float eta = v[c + j];
+            float term, resid;
+            if (LINK == LINK_LOGIT) {
+              const float e = __expf(-fabsf(eta));
+              const float d = 1.f + e;
+              const float inv = __fdividef(1.f, d);
+              const float sig = eta >= 0.f ? inv : e * inv;
+              term = yv * eta - (fmaxf(eta, 0.f) + __logf(d));
+              resid = yv - sig;
+            } else {
+              const float mu = __expf(eta);
+              term = yv * eta - mu;
+              resid = yv - mu;
+            }
+            v[c + j] = valid ? term : 0.f;
+            res[j] = valid ? resid : 0.f;
+          }
+          const __nv_bfloat162 hp = __floats2bfloat162_rn(res[0], res[1]);
+          const float2 hf = __bfloat1622float2(hp);
+          const __nv_bfloat162 lp2 = __floats2bfloat162_rn(res[0] - hf.x, res[1] - hf.y);
+          rh[c >> 1] = *reinterpret_cast<const uint32_t*>(&hp);
+          rl[c >> 1] = *reinterpret_cast<const uint32_t*>(&lp2);
+        }
+        if (!warp_wait(&bars[B_REMPTY], (i & 1) ^ 1, abort_s, a.err, 16)) {
+          ok = false;
+          break;
+        }
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          const int cg = 4 * h + g;  // chain group of 8
+          const uint32_t off = (uint32_t)(cg * ((TM / 8) * 128) + (r >> 3) * 128 + (r & 7) * 16);
+          *reinterpret_cast<uint4*>(sRh + off) =
+              make_uint4(rh[4 * g], rh[4 * g + 1], rh[4 * g + 2], rh[4 * g + 3]);
+          *reinterpret_cast<uint4*>(sRl + off) =
+              make_uint4(rl[4 * g], rl[4 * g + 1], rl[4 * g + 2], rl[4 * g + 3]);
+        }
+        fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bars[B_RFULL]);
+        lp_acc += (double)warp_reduce_scatter32(v);
+      }
+      sLP[q * NC + 32 * h + lane] = lp_acc;
+      // gradient partials: this thread's feature row of G, 32 chains
+      if (ok && warp_wait(&bars[B_D2FULL], 0, abort_s, a.err, 17)) {
+        fence_after_sync();
+        float g[32];
+        tmem_ld32(tD2 + 32 * h + ((uint32_t)(q * 32) << 16), g);
+        tmem_ld_wait();
+        const int k = q * 32 + lane;
+        int slot = -1;
+        if (k < hb)
+          slot = 1;
+        else if (k - hb < a.K)
+          slot = 4 + (k - hb);
+        if (slot >= 0) {
+#pragma unroll
+          for (int c = 0; c < 32; ++c)
+            if (act_s[32 * h + c])
+              a.P[((size_t)s * a.C + c0 + 32 * h + c) * a.NP + slot] = (double)g[c];
+        }
+      }
     }
   }
   fence_before_sync();
   __syncthreads();
+  if (tid < NC && act_s[tid]) {
+    double* dst = a.P + ((size_t)s * a.C + c0 + tid) * a.NP;
+    double lp = 0.0;
+    if (n > 0) lp = sLP[tid] + sLP[NC + tid] + sLP[2 * NC + tid] + sLP[3 * NC + tid];
+    dst[0] = lp;
+    dst[2] = 0.0;
+    dst[3] = 0.0;
+    if (n == 0) {
+      for (int k = 0; k < Kx; ++k) dst[k < hb ? 1 : 4 + (k - hb)] = 0.0;
+    }
+  }
   if (warp == 0) {
     fence_after_sync();
-    tmem_dealloc(tmem, 128);
+    tmem_dealloc(tmem, 256);
   }
 }
 
@@ -374,8 +425,14 @@ int launch_tc(const ModelDesc& m, const double* Q, int ldq, int C, const int* ac
               GradWorkspace& ws, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      SMEM_ALLOC));
+    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tc_kernel<LINK_LOGIT, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
+    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tc_kernel<LINK_LOGIT, false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
+    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tc_kernel<LINK_POISSON_LOG, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
+    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tc_kernel<LINK_POISSON_LOG, false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
     attr = true;
   }
   TcArgs a;
@@ -396,7 +453,17 @@ int launch_tc(const ModelDesc& m, const double* Q, int ldq, int C, const int* ac
   a.S = ws.S;
   a.err = ws.err;
   dim3 grid(ws.S, (C + NC - 1) / NC);
-  glm_tc_kernel<<<grid, 128, SMEM_ALLOC, st>>>(a);
+  if (m.link == LINK_LOGIT) {
+    if (a.x_has_lo)
+      glm_tc_kernel<LINK_LOGIT, true><<<grid, TC_THREADS, SMEM_ALLOC, st>>>(a);
+    else
+      glm_tc_kernel<LINK_LOGIT, false><<<grid, TC_THREADS, SMEM_ALLOC, st>>>(a);
+  } else {
+    if (a.x_has_lo)
+      glm_tc_kernel<LINK_POISSON_LOG, true><<<grid, TC_THREADS, SMEM_ALLOC, st>>>(a);
+    else
+      glm_tc_kernel<LINK_POISSON_LOG, false><<<grid, TC_THREADS, SMEM_ALLOC, st>>>(a);
+  }
   GBN_CUDA_TRY(cudaGetLastError());
   return GBNUTS_OK;
 }

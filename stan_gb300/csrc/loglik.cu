@@ -281,54 +281,56 @@ __global__ void __launch_bounds__(kThreads)
 
 static constexpr double kLogSqrt2Pi = 0.91893853320467274178032973640562;
 
-// Per chain: split sums + priors + Jacobians -> lp, grad.
+// Per chain (one warp): split sums + priors + Jacobians -> lp, grad.
 __global__ void __launch_bounds__(128)
     loglik_finalize_kernel(ModelDesc m, const double* __restrict__ Q, int ldq, int C,
                            const int* __restrict__ active, const double* __restrict__ P,
                            int NP, int S, const double* __restrict__ Gz,
                            double* __restrict__ lp_out, double* __restrict__ grad, int ldg,
                            int propto, int jacobian) {
-  const int c = blockIdx.x;
+  const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (c >= C) return;
   if (active && !active[c]) return;
-  const int tid = threadIdx.x;
   const double* th = Q + (size_t)c * ldq;
+  const size_t pstride = (size_t)C * NP;
+  const double* Pc = P + (size_t)c * NP;
   const double tau = m.idx_tau >= 0 ? exp(th[m.idx_tau]) : 0.0;
   const double jac = jacobian ? 1.0 : 0.0;
   double prior = 0.0;
-  for (int d = tid; d < m.D; d += blockDim.x) {
+  for (int d = lane; d < m.D; d += 32) {
     const double t = th[d];
     double g;
     if (d >= m.off_beta) {
       const int k = d - m.off_beta;
       double sum = 0;
-      for (int s = 0; s < S; ++s) sum += P[((size_t)s * C + c) * NP + 4 + k];
+      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 4 + k];
       g = sum - t / (m.s_beta * m.s_beta);
-      double z = t / m.s_beta;
+      const double z = t / m.s_beta;
       prior += -0.5 * z * z;
       if (!propto) prior += -log(m.s_beta) - kLogSqrt2Pi;
     } else if (d == 0 && m.has_base) {
       double sum = 0;
-      for (int s = 0; s < S; ++s) sum += P[((size_t)s * C + c) * NP + 1];
+      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 1];
       g = sum - t / (m.s_base * m.s_base);
-      double z = t / m.s_base;
+      const double z = t / m.s_base;
       prior += -0.5 * z * z;
       if (!propto) prior += -log(m.s_base) - kLogSqrt2Pi;
     } else if (d == m.idx_tau) {
       double sum = 0;
-      for (int s = 0; s < S; ++s) sum += P[((size_t)s * C + c) * NP + 2];
+      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 2];
       g = tau * (sum - tau / (m.s_tau * m.s_tau)) + jac;
-      double z = tau / m.s_tau;
+      const double z = tau / m.s_tau;
       prior += -0.5 * z * z + jac * t;
       if (!propto) prior += -log(m.s_tau) - kLogSqrt2Pi;
     } else if (d == m.idx_sigma) {
       const double sigma = exp(t);
       double sum = 0;
-      for (int s = 0; s < S; ++s) sum += P[((size_t)s * C + c) * NP + 3];
+      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 3];
       const double dsig = -(double)m.N / sigma + sum / (sigma * sigma * sigma) -
                           sigma / (m.s_sigma * m.s_sigma);
       g = sigma * dsig + jac;
-      double z = sigma / m.s_sigma;
+      const double z = sigma / m.s_sigma;
       prior += -0.5 * z * z + jac * t - (double)m.N * t;
       if (!propto) prior += -log(m.s_sigma) - kLogSqrt2Pi;
     } else {  // z_j
@@ -339,17 +341,12 @@ __global__ void __launch_bounds__(128)
     }
     grad[(size_t)c * ldg + d] = g;
   }
-  __shared__ double red[128];
-  red[tid] = prior;
-  __syncthreads();
-  for (int w = 64; w > 0; w >>= 1) {
-    if (tid < w) red[tid] += red[tid + w];
-    __syncthreads();
-  }
-  if (tid == 0) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) prior += __shfl_xor_sync(0xffffffffu, prior, off);
+  if (lane == 0) {
     double sum = 0;
-    for (int s = 0; s < S; ++s) sum += P[((size_t)s * C + c) * NP + 0];
-    double lp = sum + red[0];
+    for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 0];
+    double lp = sum + prior;
     if (!propto) {
       if (m.link == LINK_NORMAL) lp += -(double)m.N * kLogSqrt2Pi;
       if (m.link == LINK_POISSON_LOG) lp += -m.sum_lgamma_y;
@@ -498,9 +495,9 @@ int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int
   }
   GBN_CUDA_TRY(cudaGetLastError());
   if (ev1) cudaEventRecord(ev1, stream);
-  loglik_finalize_kernel<<<C, 128, 0, stream>>>(m, Q, ldq, C, active, ws.partial, ws.NP,
-                                                ws.S, ws.gz, lp, grad, ldg, propto,
-                                                jacobian);
+  loglik_finalize_kernel<<<(C + 3) / 4, 128, 0, stream>>>(m, Q, ldq, C, active, ws.partial,
+                                                          ws.NP, ws.S, ws.gz, lp, grad, ldg,
+                                                          propto, jacobian);
   GBN_CUDA_TRY(cudaGetLastError());
   return GBNUTS_OK;
 }
