@@ -110,6 +110,20 @@ int gbnuts_log_prob_grad_batch_device(gbnuts_model* m, int C, const double* d_th
                                       double* d_lp, double* d_grad, int precision,
                                       void* stream);
 
+/* The batched gradient above without any device allocation.  No counterpart
+ * in the reference: it is for callers that cannot allocate device memory when
+ * they need a gradient (a host that reserved the device's memory up front for
+ * its own pool, code running under another framework's allocator lock, a loop
+ * that cannot afford an allocation's implicit synchronisation).  Instead of
+ * the handle's workspace it uses one fixed 16 MiB device array in the library;
+ * requests needing more (many chains x many features) are rejected with
+ * GBNUTS_USAGE.  fp64 and fp32 precisions only.  The first call on each device
+ * looks up that array's address and should come before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race. */
+int gbnuts_log_prob_grad_batch_device_noalloc(gbnuts_model* m, int C, const double* d_theta,
+                                              double* d_lp, double* d_grad, int precision,
+                                              void* stream);
+
 /* write_array (model_base.hpp:370): unconstrained -> constrained (tau, sigma = exp). */
 int gbnuts_write_array(const gbnuts_model* m, const double* theta_unc, double* out);
 

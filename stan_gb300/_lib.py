@@ -81,6 +81,10 @@ SIGNATURES = {
                                                          ctypes.c_void_p, ctypes.c_void_p,
                                                          ctypes.c_void_p, ctypes.c_int,
                                                          ctypes.c_void_p]),
+    "gbnuts_log_prob_grad_batch_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int,
+                                                                 ctypes.c_void_p, ctypes.c_void_p,
+                                                                 ctypes.c_void_p, ctypes.c_int,
+                                                                 ctypes.c_void_p]),
     "gbnuts_write_array": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
     "gbnuts_unconstrain_array": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
     "gbnuts_hmc_nuts_diag_e_adapt": (ctypes.c_int, [

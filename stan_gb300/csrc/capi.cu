@@ -114,6 +114,15 @@ static int ensure_scratch(gbnuts_model* m, int C) {
   return GBNUTS_OK;
 }
 
+// Read-only view of a model for the no-allocation entry point (noalloc.cu).
+int gbnuts_internal_model_view(const gbnuts_model* m, gbn::ModelDesc* desc,
+                               const int** group_off) {
+  if (!m) return fail(GBNUTS_USAGE, "model is NULL");
+  *desc = m->desc;
+  *group_off = m->h_group_off.empty() ? nullptr : m->h_group_off.data();
+  return GBNUTS_OK;
+}
+
 extern "C" {
 
 int gbnuts_last_error(char* buf, int cap) {

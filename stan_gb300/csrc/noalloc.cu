@@ -1,0 +1,154 @@
+// Batched log density and gradient without any device allocation.
+//
+// Who needs this: code that may not call cudaMalloc at the moment it needs a
+// gradient, for example a host that has reserved all device memory up front
+// for its own pool, a callback running inside another framework's allocator
+// lock, or a latency-critical loop where an allocation (and the implicit
+// synchronisation it can cause) is not acceptable.  The regular batched entry
+// point grows a workspace owned by the model handle with cudaMalloc on first
+// use and whenever the chain count changes; this one never does.
+//
+// The scratch it needs (per row split and chain: the partial sums of lp and of
+// the gradient; per chain and group: the group sums; the split boundaries and
+// an error flag) lives in one file-scope device array of fixed size,
+// kNoAllocScratchBytes.  Every GPU that loads the library holds that array
+// until the process exits.  All calls on a device share it and it keeps the
+// last call's contents, so the parts that must start at zero are cleared on
+// every call, and two calls that overlap on the GPU (different streams, or
+// different host threads without ordering) race on it.
+//
+// The device address of the array is obtained once per device, with that
+// device current, on the first call made on that device; that first call
+// should therefore be made before any stream capture begins.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+
+#include "../../include/gbnuts.h"
+#include "gbnuts_internal.h"
+
+namespace gbn {
+
+// 16 MiB: enough for, e.g., 1024 chains x K = 100 x 19 row splits, or 256
+// chains of a 2000-group hierarchical model.
+constexpr size_t kNoAllocScratchBytes = 16u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void* g_scratch_addr[kMaxDevices] = {nullptr};
+
+// Once per device, with that device current: the device address of the array.
+int scratch_address(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_last_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    return GBNUTS_SOFTWARE;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_last_error("device index beyond the no-allocation entry point's table");
+    return GBNUTS_SOFTWARE;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      set_last_error(std::string("cudaGetSymbolAddress of the scratch array: ") +
+                     cudaGetErrorString(e));
+      return GBNUTS_SOFTWARE;
+    }
+    g_scratch_addr[dev] = p;
+  }
+  *out = g_scratch_addr[dev];
+  return GBNUTS_OK;
+}
+
+size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+}  // namespace
+
+}  // namespace gbn
+
+// Reads the model descriptor and the host copy of the group offsets; declared
+// in capi.cu beside the model handle.
+int gbnuts_internal_model_view(const gbnuts_model* m, gbn::ModelDesc* desc,
+                               const int** group_off);
+
+extern "C" int gbnuts_log_prob_grad_batch_device_noalloc(gbnuts_model* m, int C,
+                                                         const double* d_theta, double* d_lp,
+                                                         double* d_grad, int precision,
+                                                         void* stream) {
+  using namespace gbn;
+  if (!m || C <= 0 || !d_theta || !d_lp || !d_grad) {
+    set_last_error("bad arguments");
+    return GBNUTS_USAGE;
+  }
+  if (precision != GBNUTS_PREC_FP64 && precision != GBNUTS_PREC_FP32) {
+    set_last_error("the no-allocation entry point supports the fp64 and fp32 forms only");
+    return GBNUTS_USAGE;
+  }
+  ModelDesc desc;
+  const int* group_off = nullptr;
+  int rc = gbnuts_internal_model_view(m, &desc, &group_off);
+  if (rc) return rc;
+  const int CB = chains_per_block(desc.K);
+  if (CB == 0) {
+    set_last_error("K beyond the supported maximum (2048)");
+    return GBNUTS_USAGE;
+  }
+  // Row splits exactly as the regular entry point chooses them.
+  const int chain_blocks = (C + CB - 1) / CB;
+  long long max_s = std::max(1LL, desc.N / 64);
+  int S = (int)std::min<long long>(max_s, std::max(1, (2 * 152 + chain_blocks - 1) / chain_blocks));
+  if (desc.off_z >= 0) S = std::min(S, desc.J);
+  S = std::max(S, 1);
+  constexpr int kMaxSplits = 512;
+  if (S > kMaxSplits) S = kMaxSplits;
+  const int NP = n_partials(desc);
+  const size_t partial_bytes = align256((size_t)S * C * NP * sizeof(double));
+  const size_t gz_bytes = desc.off_z >= 0 ? align256((size_t)C * desc.J * sizeof(double)) : 0;
+  const size_t split_bytes = align256((size_t)(S + 1) * sizeof(long long));
+  const size_t need = partial_bytes + gz_bytes + split_bytes + 256;
+  if (need > kNoAllocScratchBytes) {
+    set_last_error("the request needs " + std::to_string(need) +
+                   " bytes of scratch; the no-allocation entry point has " +
+                   std::to_string(kNoAllocScratchBytes) + " (use fewer chains per call)");
+    return GBNUTS_USAGE;
+  }
+  void* base = nullptr;
+  rc = scratch_address(&base);
+  if (rc) return rc;
+  unsigned char* b = static_cast<unsigned char*>(base);
+  GradWorkspace ws;
+  ws.C = C;
+  ws.S = S;
+  ws.NP = NP;
+  ws.precision = precision;
+  ws.partial = reinterpret_cast<double*>(b);
+  ws.gz = desc.off_z >= 0 ? reinterpret_cast<double*>(b + partial_bytes) : nullptr;
+  ws.split_rows = reinterpret_cast<long long*>(b + partial_bytes + gz_bytes);
+  ws.err = reinterpret_cast<int*>(b + partial_bytes + gz_bytes + split_bytes);
+  long long rows[kMaxSplits + 1];
+  for (int s = 0; s <= S; ++s) {
+    if (desc.off_z >= 0)
+      rows[s] = group_off[(long long)desc.J * s / S];
+    else
+      rows[s] = desc.N * s / S;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemcpyAsync(ws.split_rows, rows, (S + 1) * sizeof(long long),
+                                  cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws.err, 0, sizeof(int), st);
+  if (e != cudaSuccess) {
+    set_last_error(std::string("scratch set-up: ") + cudaGetErrorString(e));
+    return GBNUTS_SOFTWARE;
+  }
+  // The group sums are cleared by the launch itself; the partials are fully
+  // overwritten for every active chain.
+  return launch_log_prob_grad(desc, precision, d_theta, desc.D, C, nullptr, d_lp, d_grad,
+                              desc.D, 1, 1, ws, st, nullptr, nullptr);
+}
