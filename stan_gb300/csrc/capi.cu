@@ -507,14 +507,14 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   cudaStream_t st = m->stream;
   DeviceRun dr;
   ChainState* d_states;
-  double *d_vecs, *d_req, *d_lp, *d_grad, *d_draws, *d_diag = nullptr, *d_init, *d_inits = nullptr,
-                                                   *d_invm = nullptr;
+  ChainStack* d_stacks;
+  double *d_vecs, *d_req, *d_draws, *d_diag = nullptr, *d_init, *d_inits = nullptr,
+                                    *d_invm = nullptr;
   int *d_active, *d_done, *d_abort;
   GBN_CUDA_TRY(dr.alloc(&d_states, C));
+  GBN_CUDA_TRY(dr.alloc(&d_stacks, C));
   GBN_CUDA_TRY(dr.alloc(&d_vecs, (size_t)C * cfg.n_slots * cfg.ld));
   GBN_CUDA_TRY(dr.alloc(&d_req, (size_t)C * cfg.ld));
-  GBN_CUDA_TRY(dr.alloc(&d_grad, (size_t)C * cfg.ld));
-  GBN_CUDA_TRY(dr.alloc(&d_lp, C));
   GBN_CUDA_TRY(dr.alloc(&d_active, C));
   GBN_CUDA_TRY(dr.alloc(&d_draws, (size_t)C * out->max_rows * n_cols));
   if (out->diagnostics) GBN_CUDA_TRY(dr.alloc(&d_diag, (size_t)C * out->max_rows * 3 * D));
@@ -533,56 +533,100 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   }
   GBN_CUDA_TRY(cudaMemsetAsync(d_done, 0, sizeof(int), st));
   GBN_CUDA_TRY(cudaMemsetAsync(d_abort, 0, sizeof(int), st));
-  GBN_CUDA_TRY(cudaMemsetAsync(d_grad, 0, (size_t)C * cfg.ld * sizeof(double), st));
+  GBN_CUDA_TRY(cudaMemsetAsync(d_req, 0, (size_t)C * cfg.ld * sizeof(double), st));
   GBN_CUDA_TRY(cudaMemsetAsync(d_draws, 0, (size_t)C * out->max_rows * n_cols * sizeof(double), st));
   int prc = ensure_precision(m, rc->precision);
   if (prc) return prc;
   prc = prepare_workspace(m->desc, m->h_group_off.data(), C, rc->precision, m->ws);
   if (prc) return prc;
+  const PartialsView pv{m->ws.partial, m->ws.NP, m->ws.S, m->ws.gz};
 
   int* h_done = nullptr;
   GBN_CUDA_TRY(cudaMallocHost(&h_done, sizeof(int)));
-  struct PinnedGuard {
-    int* p;
-    ~PinnedGuard() { cudaFreeHost(p); }
-  } pg{h_done};
+  struct RunGuard {
+    int* pinned = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~RunGuard() {
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+      if (pinned) cudaFreeHost(pinned);
+    }
+  } guard;
+  guard.pinned = h_done;
 
   cudaEvent_t ev_begin, ev_end;
   GBN_CUDA_TRY(cudaEventCreate(&ev_begin));
   GBN_CUDA_TRY(cudaEventCreate(&ev_end));
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> grad_events;
-  const int kSampleEvery = 16;
   const size_t kMaxSamples = 512;
 
-  launch_nuts_init(cfg, d_states, d_vecs, d_invm, d_active, d_lp, st);
+  launch_nuts_init(cfg, d_states, d_stacks, d_vecs, d_invm, d_active, st);
   GBN_CUDA_TRY(cudaGetLastError());
   GBN_CUDA_TRY(cudaEventRecord(ev_begin, st));
   auto wall0 = std::chrono::steady_clock::now();
 
+  // One step: every chain's state machine runs to its next gradient request,
+  // then the gradient stage writes split partials the next step finalises.
+  auto enqueue_step = [&](cudaEvent_t e0, cudaEvent_t e1) -> int {
+    launch_nuts_step(cfg, m->desc, d_states, d_stacks, d_vecs, d_req, pv, d_active, d_draws,
+                     d_diag, d_init, d_inits, d_done, d_abort, st);
+    return launch_partials(m->desc, rc->precision, d_req, cfg.ld, C, d_active, m->ws, st, e0,
+                           e1);
+  };
+  // Steps run in chunks of 32 captured once into a CUDA graph; every 16th
+  // chunk runs eagerly with CUDA events around the gradient kernel (its live
+  // launch time).  The first chunk is eager (it also sets kernel attributes).
+  const int kChunk = 32;
+  const int kTimedEvery = 16;
+  bool use_graph = true;
   long long step = 0;
-  const int chunk = 32;
+  const long long iters = (long long)rc->num_warmup + rc->num_samples;
   // upper bound on steps: every transition is at most 2^max_depth - 1 leapfrogs,
   // step-size searches are bounded by the 1e7 / 0 stops, 100 init tries.
-  const long long iters = (long long)rc->num_warmup + rc->num_samples;
   const long long max_steps = (iters + 2) * ((1LL << max_depth) + 200) + 1000;
+  const int launches_per_step = 2 + (m->desc.off_z >= 0 ? 1 : 0);
   int status_rc = GBNUTS_OK;
   long long launches = 0;
-  for (;;) {
-    for (int k = 0; k < chunk; ++k) {
-      launch_nuts_step(cfg, d_states, d_vecs, d_req, d_lp, d_grad, d_active, d_draws, d_diag,
-                       d_init, d_inits, d_done, d_abort, step, st);
-      cudaEvent_t e0 = nullptr, e1 = nullptr;
-      if ((step % kSampleEvery) == 0 && grad_events.size() < kMaxSamples) {
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        grad_events.emplace_back(e0, e1);
+  for (long long chunk_i = 0;; ++chunk_i) {
+    const bool eager = !use_graph || (chunk_i % kTimedEvery) == 0;
+    if (eager) {
+      for (int k = 0; k < kChunk; ++k) {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if ((k % 4) == 0 && grad_events.size() < kMaxSamples) {
+          cudaEventCreate(&e0);
+          cudaEventCreate(&e1);
+          grad_events.emplace_back(e0, e1);
+        }
+        int r = enqueue_step(e0, e1);
+        if (r) return r;
       }
-      int r = launch_log_prob_grad(m->desc, rc->precision, d_req, cfg.ld, C, d_active, d_lp,
-                                   d_grad, cfg.ld, 1, 1, m->ws, st, e0, e1);
-      if (r) return r;
-      launches += 2 + (m->desc.off_z >= 0 ? 1 : 0) + 1;
-      ++step;
+    } else {
+      if (!guard.exec) {
+        int r = GBNUTS_OK;
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+          for (int k = 0; k < kChunk && r == GBNUTS_OK; ++k) r = enqueue_step(nullptr, nullptr);
+          cudaGraph_t g = nullptr;
+          e = cudaStreamEndCapture(st, &g);
+          guard.graph = g;
+          if (e == cudaSuccess && r == GBNUTS_OK && g)
+            e = cudaGraphInstantiate(&guard.exec, g, 0);
+        }
+        if (e != cudaSuccess || r != GBNUTS_OK || !guard.exec) {
+          // capture unavailable: run every chunk eagerly
+          cudaGetLastError();
+          use_graph = false;
+          for (int k = 0; k < kChunk; ++k) {
+            int r2 = enqueue_step(nullptr, nullptr);
+            if (r2) return r2;
+          }
+        }
+      }
+      if (use_graph) GBN_CUDA_TRY(cudaGraphLaunch(guard.exec, st));
     }
+    step += kChunk;
+    launches += (long long)kChunk * launches_per_step;
     GBN_CUDA_TRY(cudaMemcpyAsync(h_done, d_done, sizeof(int), cudaMemcpyDeviceToHost, st));
     GBN_CUDA_TRY(cudaStreamSynchronize(st));
     if (*h_done >= C) break;
@@ -638,7 +682,10 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
     if (out->stepsize) out->stepsize[c] = hs[c].nom_eps;
     if (out->n_grad) out->n_grad[c] = hs[c].n_grad;
     if (out->seconds) {
-      double frac = (hs[c].warm_end_step >= 0 && step > 0) ? (double)hs[c].warm_end_step / step : 0.0;
+      // each chain's warmup share of the run, by its gradient count
+      const double frac = (hs[c].warm_end_ngrad >= 0 && hs[c].n_grad > 0)
+                              ? (double)hs[c].warm_end_ngrad / (double)hs[c].n_grad
+                              : 0.0;
       out->seconds[2 * c] = wall_s * frac;
       out->seconds[2 * c + 1] = wall_s * (1.0 - frac);
     }

@@ -71,6 +71,12 @@ int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int pre
                       GradWorkspace& ws);
 void free_workspace(GradWorkspace& ws);
 
+// The split partial sums only (no finalize), for callers that finalize
+// themselves (the sampler's step kernel).
+int launch_partials(const ModelDesc& m, int precision, const double* Q, int ldq, int C,
+                    const int* active, GradWorkspace& ws, cudaStream_t stream, cudaEvent_t ev0,
+                    cudaEvent_t ev1);
+
 // lp[C] and grad[C][ldg] of C chains at Q[C][ldq] (device pointers), with
 // Stan's propto/jacobian semantics; active (may be null) masks chains.
 int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int ldq,

@@ -25,6 +25,7 @@
 
 #include "../../include/gbnuts.h"
 #include "gbnuts_internal.h"
+#include "loglik_finalize.cuh"
 
 namespace gbn {
 
@@ -279,8 +280,6 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-static constexpr double kLogSqrt2Pi = 0.91893853320467274178032973640562;
-
 // Per chain (one warp): split sums + priors + Jacobians -> lp, grad.
 __global__ void __launch_bounds__(128)
     loglik_finalize_kernel(ModelDesc m, const double* __restrict__ Q, int ldq, int C,
@@ -292,67 +291,9 @@ __global__ void __launch_bounds__(128)
   const int lane = threadIdx.x & 31;
   if (c >= C) return;
   if (active && !active[c]) return;
-  const double* th = Q + (size_t)c * ldq;
-  const size_t pstride = (size_t)C * NP;
-  const double* Pc = P + (size_t)c * NP;
-  const double tau = m.idx_tau >= 0 ? exp(th[m.idx_tau]) : 0.0;
-  const double jac = jacobian ? 1.0 : 0.0;
-  double prior = 0.0;
-  for (int d = lane; d < m.D; d += 32) {
-    const double t = th[d];
-    double g;
-    if (d >= m.off_beta) {
-      const int k = d - m.off_beta;
-      double sum = 0;
-      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 4 + k];
-      g = sum - t / (m.s_beta * m.s_beta);
-      const double z = t / m.s_beta;
-      prior += -0.5 * z * z;
-      if (!propto) prior += -log(m.s_beta) - kLogSqrt2Pi;
-    } else if (d == 0 && m.has_base) {
-      double sum = 0;
-      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 1];
-      g = sum - t / (m.s_base * m.s_base);
-      const double z = t / m.s_base;
-      prior += -0.5 * z * z;
-      if (!propto) prior += -log(m.s_base) - kLogSqrt2Pi;
-    } else if (d == m.idx_tau) {
-      double sum = 0;
-      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 2];
-      g = tau * (sum - tau / (m.s_tau * m.s_tau)) + jac;
-      const double z = tau / m.s_tau;
-      prior += -0.5 * z * z + jac * t;
-      if (!propto) prior += -log(m.s_tau) - kLogSqrt2Pi;
-    } else if (d == m.idx_sigma) {
-      const double sigma = exp(t);
-      double sum = 0;
-      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 3];
-      const double dsig = -(double)m.N / sigma + sum / (sigma * sigma * sigma) -
-                          sigma / (m.s_sigma * m.s_sigma);
-      g = sigma * dsig + jac;
-      const double z = sigma / m.s_sigma;
-      prior += -0.5 * z * z + jac * t - (double)m.N * t;
-      if (!propto) prior += -log(m.s_sigma) - kLogSqrt2Pi;
-    } else {  // z_j
-      const int j = d - m.off_z;
-      g = tau * Gz[(size_t)c * m.J + j] - t;
-      prior += -0.5 * t * t;
-      if (!propto) prior += -kLogSqrt2Pi;
-    }
-    grad[(size_t)c * ldg + d] = g;
-  }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) prior += __shfl_xor_sync(0xffffffffu, prior, off);
-  if (lane == 0) {
-    double sum = 0;
-    for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 0];
-    double lp = sum + prior;
-    if (!propto) {
-      if (m.link == LINK_NORMAL) lp += -(double)m.N * kLogSqrt2Pi;
-      if (m.link == LINK_POISSON_LOG) lp += -m.sum_lgamma_y;
-    }
-    lp_out[c] = lp;
-  }
+  const double lp = finalize_chain(m, Q + (size_t)c * ldq, c, C, P, NP, S, Gz,
+                                   grad + (size_t)c * ldg, 1.0, propto, jacobian, lane);
+  if (lane == 0) lp_out[c] = lp;
 }
 
 // ------------------------------------------------------------------ host side
@@ -475,10 +416,9 @@ void free_workspace(GradWorkspace& ws) {
   ws = GradWorkspace();
 }
 
-int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int ldq,
-                         int C, const int* active, double* lp, double* grad, int ldg,
-                         int propto, int jacobian, GradWorkspace& ws,
-                         cudaStream_t stream, cudaEvent_t ev0, cudaEvent_t ev1) {
+int launch_partials(const ModelDesc& m, int precision, const double* Q, int ldq, int C,
+                    const int* active, GradWorkspace& ws, cudaStream_t stream, cudaEvent_t ev0,
+                    cudaEvent_t ev1) {
   if (m.off_z >= 0)
     GBN_CUDA_TRY(cudaMemsetAsync(ws.gz, 0, (size_t)C * m.J * sizeof(double), stream));
   if (ev0) cudaEventRecord(ev0, stream);
@@ -495,6 +435,15 @@ int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int
   }
   GBN_CUDA_TRY(cudaGetLastError());
   if (ev1) cudaEventRecord(ev1, stream);
+  return GBNUTS_OK;
+}
+
+int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int ldq,
+                         int C, const int* active, double* lp, double* grad, int ldg,
+                         int propto, int jacobian, GradWorkspace& ws,
+                         cudaStream_t stream, cudaEvent_t ev0, cudaEvent_t ev1) {
+  int rc = launch_partials(m, precision, Q, ldq, C, active, ws, stream, ev0, ev1);
+  if (rc) return rc;
   loglik_finalize_kernel<<<(C + 3) / 4, 128, 0, stream>>>(m, Q, ldq, C, active, ws.partial,
                                                           ws.NP, ws.S, ws.gz, lp, grad, ldg,
                                                           propto, jacobian);

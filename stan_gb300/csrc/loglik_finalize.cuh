@@ -1,0 +1,82 @@
+// Finalisation of one chain's log density and gradient from the split
+// partial sums: split sums in split order (deterministic), priors, the
+// Jacobian of tau = exp(u), sigma = exp(u), and the chain rule through them.
+// One warp per chain, lanes over the coordinates; returns lp in every lane.
+// Shared by the batched-gradient finalize kernel and the sampler step kernel.
+#pragma once
+
+#include <math.h>
+
+#include "gbnuts_internal.h"
+
+namespace gbn {
+
+static constexpr double kLogSqrt2Pi = 0.91893853320467274178032973640562;
+
+// th: the chain's parameters; grad_out[d] = sign * d lp / d theta_d.
+__device__ __forceinline__ double finalize_chain(const ModelDesc& m, const double* th, int c,
+                                                 int C, const double* __restrict__ P, int NP,
+                                                 int S, const double* __restrict__ Gz,
+                                                 double* grad_out, double sign, int propto,
+                                                 int jacobian, int lane) {
+  const size_t pstride = (size_t)C * NP;
+  const double* Pc = P + (size_t)c * NP;
+  const double tau = m.idx_tau >= 0 ? exp(th[m.idx_tau]) : 0.0;
+  const double jac = jacobian ? 1.0 : 0.0;
+  double prior = 0.0;
+  for (int d = lane; d < m.D; d += 32) {
+    const double t = th[d];
+    double g;
+    if (d >= m.off_beta) {
+      const int k = d - m.off_beta;
+      double sum = 0;
+      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 4 + k];
+      g = sum - t / (m.s_beta * m.s_beta);
+      const double z = t / m.s_beta;
+      prior += -0.5 * z * z;
+      if (!propto) prior += -log(m.s_beta) - kLogSqrt2Pi;
+    } else if (d == 0 && m.has_base) {
+      double sum = 0;
+      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 1];
+      g = sum - t / (m.s_base * m.s_base);
+      const double z = t / m.s_base;
+      prior += -0.5 * z * z;
+      if (!propto) prior += -log(m.s_base) - kLogSqrt2Pi;
+    } else if (d == m.idx_tau) {
+      double sum = 0;
+      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 2];
+      g = tau * (sum - tau / (m.s_tau * m.s_tau)) + jac;
+      const double z = tau / m.s_tau;
+      prior += -0.5 * z * z + jac * t;
+      if (!propto) prior += -log(m.s_tau) - kLogSqrt2Pi;
+    } else if (d == m.idx_sigma) {
+      const double sigma = exp(t);
+      double sum = 0;
+      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 3];
+      const double dsig = -(double)m.N / sigma + sum / (sigma * sigma * sigma) -
+                          sigma / (m.s_sigma * m.s_sigma);
+      g = sigma * dsig + jac;
+      const double z = sigma / m.s_sigma;
+      prior += -0.5 * z * z + jac * t - (double)m.N * t;
+      if (!propto) prior += -log(m.s_sigma) - kLogSqrt2Pi;
+    } else {  // z_j
+      const int j = d - m.off_z;
+      g = tau * Gz[(size_t)c * m.J + j] - t;
+      prior += -0.5 * t * t;
+      if (!propto) prior += -kLogSqrt2Pi;
+    }
+    grad_out[d] = sign * g;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) prior += __shfl_xor_sync(0xffffffffu, prior, off);
+  double sum = 0;
+  for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 0];
+  double lp = sum + prior;
+  if (!propto) {
+    if (m.link == LINK_NORMAL) lp += -(double)m.N * kLogSqrt2Pi;
+    if (m.link == LINK_POISSON_LOG) lp += -m.sum_lgamma_y;
+  }
+  return lp;
+}
+
+}  // namespace gbn

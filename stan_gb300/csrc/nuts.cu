@@ -31,6 +31,8 @@
 
 #include "../../include/gbnuts.h"
 #include "../../include/gbnuts_draw_stream.h"
+#include "gbnuts_internal.h"
+#include "loglik_finalize.cuh"
 #include "nuts_device.h"
 
 namespace gbn {
@@ -67,6 +69,15 @@ struct Ctx {
   __device__ double* slot(int s) const {
     return vecs + ((size_t)c * cfg.n_slots + s) * cfg.ld;
   }
+};
+
+// The chain's per-level stack in shared memory (one copy per warp).  All
+// lanes hold the same values; entries read and then rewritten by every lane
+// are separated by __syncwarp so no lane reads another lane's new value.
+struct Stk {
+  double* lsw;
+  double* V;
+  int* slot;
 };
 
 // T(p) = 1/2 p . (invM p)  (diag_e_metric.hpp:20-22)
@@ -109,15 +120,6 @@ static __device__ void drift_and_request(const Ctx& x, double* q, const double* 
     q[i] = v;
     req[i] = v;
   }
-}
-
-// V = -lp, g = -grad lp; a non-finite lp rejects the point (base_hamiltonian.hpp:61-70).
-static __device__ double take_gradient(const Ctx& x, double lp, const double* grad,
-                                       double* g) {
-  for (int i = x.lane; i < x.cfg.D; i += 32) g[i] = -grad[i];
-  if (isnan(lp)) return lp;
-  if (!isfinite(lp)) return __longlong_as_double(0x7ff0000000000000LL);
-  return -lp;
 }
 
 // constrained output (write_array): exp for the positive parameters.
@@ -226,10 +228,11 @@ static __device__ int learn_variance(const Ctx& x, ChainState& st) {
 // Merges the subtree `cur` (the working leaf, or stack level cur_level) into
 // stack level l (its left sibling), as build_tree does after its final
 // subtree returns (base_nuts.hpp:321-351).  Returns the U-turn verdict.
-static __device__ bool merge_into_level(const Ctx& x, ChainState& st, int l, int cur_level,
-                                        int wq, int wp, int wg, double cur_lsw, double cur_V) {
+static __device__ bool merge_into_level(const Ctx& x, ChainState& st, const Stk& sk, int l,
+                                        int cur_level, int wq, int wp, int wg, double cur_lsw,
+                                        double cur_V) {
   const SamplerCfg& cfg = x.cfg;
-  const int pi = st.slot_of[l];
+  const int pi = sk.slot[l];
   const int base_i = SL_STACK + 6 * pi;
   double* IQ = x.slot(base_i + 0);
   double* IP = x.slot(base_i + 1);
@@ -246,7 +249,7 @@ static __device__ bool merge_into_level(const Ctx& x, ChainState& st, int l, int
     CPE = CP;
     CR = CP;
   } else {
-    const int base_c = SL_STACK + 6 * st.slot_of[cur_level];
+    const int base_c = SL_STACK + 6 * sk.slot[cur_level];
     CQ = x.slot(base_c + 0);
     CP = x.slot(base_c + 1);
     CG = x.slot(base_c + 2);
@@ -254,7 +257,7 @@ static __device__ bool merge_into_level(const Ctx& x, ChainState& st, int l, int
     CPE = x.slot(base_c + 4);
     CR = x.slot(base_c + 5);
   }
-  const double init_lsw = st.stack_lsw[l];
+  const double init_lsw = sk.lsw[l];
   const double lsw_sub = log_sum_exp_d(init_lsw, cur_lsw);
   bool sel_final;
   if (cur_lsw > lsw_sub) {
@@ -289,20 +292,22 @@ static __device__ bool merge_into_level(const Ctx& x, ChainState& st, int l, int
       IG[i] = CG[i];
     }
   }
-  if (sel_final) st.stack_V[l] = cur_V;
-  st.stack_lsw[l] = lsw_sub;
   d1a = warp_sum(d1a);
   d1b = warp_sum(d1b);
   d2a = warp_sum(d2a);
   d2b = warp_sum(d2b);
   d3a = warp_sum(d3a);
   d3b = warp_sum(d3b);
+  __syncwarp();
+  if (sel_final) sk.V[l] = cur_V;
+  sk.lsw[l] = lsw_sub;
+  __syncwarp();
   return (d1a > 0 && d1b > 0) && (d2a > 0 && d2b > 0) && (d3a > 0 && d3b > 0);
 }
 
 // Top-level merge of a completed subtree (base_nuts.hpp:157-192).
-static __device__ bool merge_top(const Ctx& x, ChainState& st, int cur_level, int wq, int wp,
-                                 int wg, double cur_lsw, double cur_V) {
+static __device__ bool merge_top(const Ctx& x, ChainState& st, const Stk& sk, int cur_level,
+                                 int wq, int wp, int wg, double cur_lsw, double cur_V) {
   const SamplerCfg& cfg = x.cfg;
   const double *CQ, *CP, *CG, *CPB, *CPE, *CR;
   if (cur_level < 0) {
@@ -313,7 +318,7 @@ static __device__ bool merge_top(const Ctx& x, ChainState& st, int cur_level, in
     CPE = CP;
     CR = CP;
   } else {
-    const int base_c = SL_STACK + 6 * st.slot_of[cur_level];
+    const int base_c = SL_STACK + 6 * sk.slot[cur_level];
     CQ = x.slot(base_c + 0);
     CP = x.slot(base_c + 1);
     CG = x.slot(base_c + 2);
@@ -398,30 +403,48 @@ static __device__ void finish_chain(ChainState& st, int status, int* done_count,
 }
 
 __global__ void __launch_bounds__(128)
-    nuts_step_kernel(SamplerCfg cfg, ChainState* __restrict__ states, double* vecs,
-                     double* __restrict__ req, const double* __restrict__ lp_in,
-                     const double* __restrict__ grad_in, int* __restrict__ active,
-                     double* __restrict__ draws, double* __restrict__ diag,
-                     double* __restrict__ init_out, const double* __restrict__ inits,
-                     int* __restrict__ done_count, const int* __restrict__ abort_flag,
-                     long long step) {
+    nuts_step_kernel(SamplerCfg cfg, ModelDesc m, ChainState* __restrict__ states,
+                     ChainStack* __restrict__ stacks, double* vecs, double* __restrict__ req,
+                     PartialsView pv, int* __restrict__ active, double* __restrict__ draws,
+                     double* __restrict__ diag, double* __restrict__ init_out,
+                     const double* __restrict__ inits, int* __restrict__ done_count,
+                     const int* __restrict__ abort_flag) {
+  __shared__ double sh_lsw[4][MAX_TREE_DEPTH];
+  __shared__ double sh_V[4][MAX_TREE_DEPTH];
+  __shared__ int sh_slot[4][MAX_TREE_DEPTH];
   const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
+  const int wl = threadIdx.x >> 5;
   if (c >= cfg.C) return;
   ChainState st = states[c];
   if (st.done) {
     if (lane == 0) active[c] = 0;
     return;
   }
+  if (lane < MAX_TREE_DEPTH) {
+    sh_lsw[wl][lane] = stacks[c].lsw[lane];
+    sh_slot[wl][lane] = stacks[c].slot[lane];
+  } else {
+    sh_V[wl][lane - MAX_TREE_DEPTH] = stacks[c].V[lane - MAX_TREE_DEPTH];
+  }
+  __syncwarp();
+  const Stk sk{sh_lsw[wl], sh_V[wl], sh_slot[wl]};
   Ctx x{cfg, vecs, c, lane};
   const int D = cfg.D;
   double* rq = req + (size_t)c * cfg.ld;
-  const double* gin = grad_in + (size_t)c * cfg.ld;
-  const double lp = lp_in[c];
   const double inf = __longlong_as_double(0x7ff0000000000000LL);
   const double log08 = log(0.8);
   bool yield = false;
   int guard = 0;
+  // The gradient requested at the previous yield, finalised from the split
+  // partials into the working point's g slot (g = -grad lp); returns V.
+  auto resume = [&](int q_slot, int g_slot) -> double {
+    const double lp = finalize_chain(m, x.slot(q_slot), c, cfg.C, pv.P, pv.NP, pv.S, pv.Gz,
+                                     x.slot(g_slot), -1.0, 1, 1, lane);
+    if (isnan(lp)) return lp;
+    if (!isfinite(lp)) return inf;
+    return -lp;
+  };
 
   while (!yield && !st.done) {
     if (++guard > 64) {
@@ -453,12 +476,15 @@ __global__ void __launch_bounds__(128)
       }
       case PH_INIT_EVAL: {
         st.n_grad += 1;
+        const double V0 = resume(SL_FWD_Q, SL_FWD_G);
         double gs = 0.0;
-        for (int i = lane; i < D; i += 32) gs += gin[i];
+        const double* g0 = x.slot(SL_FWD_G);
+        for (int i = lane; i < D; i += 32) gs += g0[i];
         gs = warp_sum(gs);
-        if (isfinite(lp) && isfinite(gs)) {
+        if (isfinite(V0) && isfinite(gs)) {
           copy_vec(x, x.slot(SL_SMP_Q), x.slot(SL_FWD_Q));
-          st.V_smp = take_gradient(x, lp, gin, x.slot(SL_SMP_G));
+          copy_vec(x, x.slot(SL_SMP_G), x.slot(SL_FWD_G));
+          st.V_smp = V0;
           if (init_out) copy_vec(x, init_out + (size_t)c * D, x.slot(SL_SMP_Q));
           if (cfg.adapt) {
             st.ss_ctx = SS_CTX_START;
@@ -508,7 +534,7 @@ __global__ void __launch_bounds__(128)
         st.n_grad += 1;
         double* p = x.slot(SL_FWD_P);
         double* g = x.slot(SL_FWD_G);
-        st.V_fwd = take_gradient(x, lp, gin, g);
+        st.V_fwd = resume(SL_FWD_Q, SL_FWD_G);
         half_kick(x, p, g, 0.5 * st.nom_eps);
         __syncwarp();
         double h = kinetic(x, p) + st.V_fwd;
@@ -556,9 +582,9 @@ __global__ void __launch_bounds__(128)
           // disengage_adaptation (adapt_diag_e_nuts.hpp:45-48)
           st.adapt_flag = 0;
           st.nom_eps = exp(st.sa_x_bar);
-          st.warm_end_step = step;
-        } else if (!cfg.adapt && st.iter == cfg.num_warmup && st.warm_end_step < 0) {
-          st.warm_end_step = step;
+          st.warm_end_ngrad = st.n_grad;
+        } else if (!cfg.adapt && st.iter == cfg.num_warmup && st.warm_end_ngrad < 0) {
+          st.warm_end_ngrad = st.n_grad;
         }
         if (st.iter >= cfg.num_warmup + cfg.num_samples) {
           finish_chain(st, GBNUTS_CHAIN_OK, done_count, lane);
@@ -626,7 +652,9 @@ __global__ void __launch_bounds__(128)
         st.dir = draw_uniform(cfg, st, c) > 0.5 ? 1 : -1;
         st.sub_d = st.depth;
         st.leaf = 0;
-        for (int l = 0; l < MAX_TREE_DEPTH; ++l) st.slot_of[l] = (unsigned char)l;
+        __syncwarp();
+        if (lane < MAX_TREE_DEPTH) sk.slot[lane] = lane;
+        __syncwarp();
         st.phase = PH_LEAF_BEGIN;
         break;
       }
@@ -650,7 +678,7 @@ __global__ void __launch_bounds__(128)
         const int wg = fwd ? SL_FWD_G : SL_BCK_G;
         double* p = x.slot(wp);
         double* g = x.slot(wg);
-        const double V = take_gradient(x, lp, gin, g);
+        const double V = resume(wq, wg);
         if (fwd)
           st.V_fwd = V;
         else
@@ -681,10 +709,10 @@ __global__ void __launch_bounds__(128)
         bool ok = true;
         while (l < d && ((i >> l) & 1)) {
           __syncwarp();
-          ok = merge_into_level(x, st, l, cur_level, wq, wp, wg, cur_lsw, cur_V);
+          ok = merge_into_level(x, st, sk, l, cur_level, wq, wp, wg, cur_lsw, cur_V);
           cur_level = l;
-          cur_lsw = st.stack_lsw[l];
-          cur_V = st.stack_V[l];
+          cur_lsw = sk.lsw[l];
+          cur_V = sk.V[l];
           ++l;
           if (!ok) break;
         }
@@ -695,7 +723,7 @@ __global__ void __launch_bounds__(128)
         if (l < d) {
           if (cur_level < 0) {
             // push the leaf as the left sibling at level 0
-            const int base_i = SL_STACK + 6 * st.slot_of[0];
+            const int base_i = SL_STACK + 6 * sk.slot[0];
             double* IQ = x.slot(base_i + 0);
             double* IP = x.slot(base_i + 1);
             double* IG = x.slot(base_i + 2);
@@ -712,22 +740,27 @@ __global__ void __launch_bounds__(128)
               IPE[k] = pk;
               IR[k] = pk;
             }
-            st.stack_lsw[0] = w;
-            st.stack_V[0] = V;
+            __syncwarp();
+            sk.lsw[0] = w;
+            sk.V[0] = V;
+            __syncwarp();
           } else {
             // the merged subtree at level l-1 becomes the left sibling at level l
-            unsigned char t = st.slot_of[l];
-            st.slot_of[l] = st.slot_of[l - 1];
-            st.slot_of[l - 1] = t;
-            st.stack_lsw[l] = st.stack_lsw[l - 1];
-            st.stack_V[l] = st.stack_V[l - 1];
+            const int sa = sk.slot[l], sb = sk.slot[l - 1];
+            const double la = sk.lsw[l - 1], va = sk.V[l - 1];
+            __syncwarp();
+            sk.slot[l] = sb;
+            sk.slot[l - 1] = sa;
+            sk.lsw[l] = la;
+            sk.V[l] = va;
+            __syncwarp();
           }
           st.leaf += 1;
           st.phase = PH_LEAF_BEGIN;
           break;
         }
         __syncwarp();
-        const bool persist = merge_top(x, st, cur_level, wq, wp, wg, cur_lsw, cur_V);
+        const bool persist = merge_top(x, st, sk, cur_level, wq, wp, wg, cur_lsw, cur_V);
         st.phase = persist ? PH_DOUBLING : PH_TRANS_END;
         break;
       }
@@ -774,6 +807,12 @@ __global__ void __launch_bounds__(128)
     __syncwarp();
   }
   __syncwarp();
+  if (lane < MAX_TREE_DEPTH) {
+    stacks[c].lsw[lane] = sk.lsw[lane];
+    stacks[c].slot[lane] = sk.slot[lane];
+  } else {
+    stacks[c].V[lane - MAX_TREE_DEPTH] = sk.V[lane - MAX_TREE_DEPTH];
+  }
   if (lane == 0) {
     states[c] = st;
     active[c] = (yield && !st.done) ? 1 : 0;
@@ -782,8 +821,8 @@ __global__ void __launch_bounds__(128)
 
 // Sets every chain's state from the configuration (service set-up,
 // hmc_nuts_diag_e_adapt.hpp:360-381).
-__global__ void nuts_init_kernel(SamplerCfg cfg, ChainState* states, double* vecs,
-                                 const double* inv_metrics, int* active, double* lp_in) {
+__global__ void nuts_init_kernel(SamplerCfg cfg, ChainState* states, ChainStack* stacks,
+                                 double* vecs, const double* inv_metrics, int* active) {
   const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (c >= cfg.C) return;
@@ -793,6 +832,11 @@ __global__ void nuts_init_kernel(SamplerCfg cfg, ChainState* states, double* vec
       v[i] = (s == SL_INVM) ? (inv_metrics ? (i < cfg.D ? inv_metrics[(size_t)c * cfg.D + i] : 1.0)
                                            : 1.0)
                             : 0.0;
+  }
+  if (lane < MAX_TREE_DEPTH) {
+    stacks[c].lsw[lane] = 0.0;
+    stacks[c].V[lane] = 0.0;
+    stacks[c].slot[lane] = lane;
   }
   if (lane == 0) {
     ChainState st;
@@ -809,32 +853,29 @@ __global__ void nuts_init_kernel(SamplerCfg cfg, ChainState* states, double* vec
     st.wa_counter = 0;
     st.wa_size = cfg.wa_size0;
     st.wa_next = cfg.wa_next0;
-    st.warm_end_step = -1;
-    for (int l = 0; l < MAX_TREE_DEPTH; ++l) st.slot_of[l] = (unsigned char)l;
+    st.warm_end_ngrad = -1;
     states[c] = st;
     active[c] = 0;
-    lp_in[c] = 0.0;
   }
 }
 
-void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, double* vecs,
-                      const double* inv_metrics, int* active, double* lp_in,
-                      cudaStream_t s) {
+void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* stacks,
+                      double* vecs, const double* inv_metrics, int* active, cudaStream_t s) {
   const int threads = 128;
   const int blocks = (int)(((size_t)cfg.C * 32 + threads - 1) / threads);
-  nuts_init_kernel<<<blocks, threads, 0, s>>>(cfg, states, vecs, inv_metrics, active, lp_in);
+  nuts_init_kernel<<<blocks, threads, 0, s>>>(cfg, states, stacks, vecs, inv_metrics, active);
 }
 
-void launch_nuts_step(const SamplerCfg& cfg, ChainState* states, double* vecs, double* req,
-                      const double* lp_in, const double* grad_in, int* active,
-                      double* draws, double* diag, double* init_out, const double* inits,
-                      int* done_count, const int* abort_flag, long long step,
+void launch_nuts_step(const SamplerCfg& cfg, const ModelDesc& m, ChainState* states,
+                      ChainStack* stacks, double* vecs, double* req, PartialsView pv,
+                      int* active, double* draws, double* diag, double* init_out,
+                      const double* inits, int* done_count, const int* abort_flag,
                       cudaStream_t s) {
   const int threads = 128;
   const int blocks = (int)(((size_t)cfg.C * 32 + threads - 1) / threads);
-  nuts_step_kernel<<<blocks, threads, 0, s>>>(cfg, states, vecs, req, lp_in, grad_in, active,
+  nuts_step_kernel<<<blocks, threads, 0, s>>>(cfg, m, states, stacks, vecs, req, pv, active,
                                               draws, diag, init_out, inits, done_count,
-                                              abort_flag, step);
+                                              abort_flag);
 }
 
 }  // namespace gbn

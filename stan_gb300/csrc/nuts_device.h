@@ -48,25 +48,39 @@ struct ChainState {
   int ss_ctx, ss_dir, ss_first, ss_fail;
   int rows, warm_rows, adapt_flag;
   unsigned long long nu, nn;  // uniforms and normals consumed
-  long long n_grad, warm_end_step;
+  long long n_grad, warm_end_ngrad;  // gradients so far; at the end of warmup
   double nom_eps, eps, H0, lsw, sum_metro, accept, energy;
   double V_fwd, V_bck, V_smp, ss_H0;
   double sa_counter, sa_s_bar, sa_x_bar, sa_mu;
   unsigned wa_num_warmup, wa_init_buffer, wa_term_buffer, wa_base_window;
   unsigned wa_counter, wa_next, wa_size;
   double w_n;
-  double stack_lsw[MAX_TREE_DEPTH];
-  double stack_V[MAX_TREE_DEPTH];
-  unsigned char slot_of[MAX_TREE_DEPTH];
 };
 
-void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, double* vecs,
-                      const double* inv_metrics, int* active, double* lp_in,
-                      cudaStream_t s);
-void launch_nuts_step(const SamplerCfg& cfg, ChainState* states, double* vecs, double* req,
-                      const double* lp_in, const double* grad_in, int* active,
-                      double* draws, double* diag, double* init_out, const double* inits,
-                      int* done_count, const int* abort_flag, long long step,
+// Per-level data of the pending left siblings (log sum weight, V of the
+// proposal, physical slot of the level), kept apart from ChainState so the
+// scalars can live in registers while these are indexed by tree level.
+struct ChainStack {
+  double lsw[MAX_TREE_DEPTH];
+  double V[MAX_TREE_DEPTH];
+  int slot[MAX_TREE_DEPTH];
+};
+
+struct ModelDesc;
+
+// Where the step kernel finds the gradient stage's split partial sums.
+struct PartialsView {
+  const double* P;
+  int NP, S;
+  const double* Gz;
+};
+
+void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* stacks,
+                      double* vecs, const double* inv_metrics, int* active, cudaStream_t s);
+void launch_nuts_step(const SamplerCfg& cfg, const ModelDesc& m, ChainState* states,
+                      ChainStack* stacks, double* vecs, double* req, PartialsView pv,
+                      int* active, double* draws, double* diag, double* init_out,
+                      const double* inits, int* done_count, const int* abort_flag,
                       cudaStream_t s);
 
 }  // namespace gbn
