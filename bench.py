@@ -225,6 +225,11 @@ def run_ours(args, ws, rank, local):
         out["e2e"] = e2e(args, ds, kw)
     if rank == 0 and not args.no_fp64:
         out["fp64_form"] = fp64_rate(model, ds, C)
+    if rank == 0 and not args.no_serving:
+        try:
+            out["serving"] = serving_leg()
+        except Exception as e:  # reported, not fatal to the headline line
+            out["serving"] = {"error": repr(e)}
     if rank == 0 and not args.no_cpu:
         eps = float(np.median(last.stepsize))
         out["cpu_baseline"] = cpu_baseline(ds, wl, args.cpu_seconds, eps,
@@ -259,6 +264,55 @@ def fp64_rate(model, ds, C):
                       precision="fp64", random_seed=7, init_radius=2.0)
     return {"grad_evals_per_s": float(res.n_grad.sum()) / (res.total_ms / 1e3),
             "sample": f"{C} chains x 20 warmup iterations", "grad_kernel_ms": res.grad_ms}
+
+
+SERVING = dict(fits=48, rate=8.0, chains=4, warmup=500, samples=500, precision="fp32",
+               steps_per_call=32, n_alone=6)
+
+
+def serving_datasets(n, seed=0):
+    """Hierarchical logistic fits of uneven size: N uniform in [2000, 20000]
+    rows, K in {8, 16, 32}, groups of 50 rows."""
+    from stan_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        N = int(rng.integers(2000, 20001))
+        K = int(rng.choice([8, 16, 32]))
+        out.append(workloads.hier_logistic(N, K, seed=100 + i))
+    return out
+
+
+def serving_leg():
+    """Continuous batching: fits arrive as a Poisson process and run in one
+    pool; p50 / p99 latency (arrival to draws on the host) and fits/s, next to
+    the same fits run one at a time through gbnuts_sample_run."""
+    from stan_gb300 import Model, sampler
+    from stan_gb300.serving import Pool, poisson_arrivals, serve
+    S = SERVING
+    dss = serving_datasets(S["fits"])
+    kw = dict(num_chains=S["chains"], num_warmup=S["warmup"], num_samples=S["samples"],
+              random_seed=1, max_depth=10, delta=0.8)
+    # warm-up: one small pooled fit (kernel attributes, first launches)
+    pool = Pool(precision=S["precision"], x_dtype="f32", max_fits=256, reserve_bytes=2 << 30)
+    pool.submit(dss[0], **dict(kw, num_warmup=20, num_samples=0))
+    pool.run_all()
+    arrivals = poisson_arrivals(S["rate"], len(dss), seed=1)
+    rep = serve(pool, dss, arrivals, steps_per_call=S["steps_per_call"], run_kwargs=kw)
+    pool.close()
+    t0 = time.time()
+    for ds in dss[:S["n_alone"]]:
+        m = Model.from_dataset(ds, x_dtype="f32")
+        sampler.run(m, precision=S["precision"], **kw)
+        m.close()
+    alone_rate = S["n_alone"] / (time.time() - t0)
+    out = rep.summary()
+    out.update(workload=f"{S['fits']} hierarchical logistic fits (N 2000-20000, K 8/16/32, "
+                        f"J = N/50), {S['chains']} chains, {S['warmup']} warmup + "
+                        f"{S['samples']} draws, {S['precision']} form",
+               arrival_rate_per_s=S["rate"], one_at_a_time_fits_per_s=alone_rate,
+               latency_unit="s")
+    return out
 
 
 def run_reference(args, ws, rank):
@@ -355,12 +409,16 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--case", default="fit", choices=["fit", "grad", "shortfit"],
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--case", default="fit", choices=["fit", "grad", "shortfit", "serving"],
                     help="fit: the benchmark; grad: two batched-gradient launches of the "
                          "workload (for kernel captures); shortfit: a fit of --short-iters "
                          "warmup iterations (for launch lists)")
     ap.add_argument("--short-iters", type=int, default=40)
     args = ap.parse_args()
+    if args.case == "serving":
+        print(json.dumps(serving_leg()))
+        return
     if args.case != "fit":
         profile_case(args)
         return

@@ -240,6 +240,44 @@ enum {
 int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* cfg,
                       gbnuts_run_output* out, const gbnuts_callbacks* cb);
 
+/* ------------------------------------------------------------ fit pool */
+
+/* Continuous batching of many fits on one GPU.  No reference counterpart:
+ * the reference's service runs one fit per call
+ * (hmc_nuts_diag_e_adapt.hpp:331-407); a pool runs each submitted fit as
+ * gbnuts_sample_run would (same draws, same chain status) while every
+ * admitted fit shares the step launches.  Forms: GBNUTS_PREC_FP64 / FP32;
+ * every fit in a pool stores X as the pool's x_dtype and has K <= 512. */
+typedef struct gbnuts_pool gbnuts_pool;
+
+/* max_fits: fits admitted at once; max_chains: chains admitted at once;
+ * reserve_bytes: device memory left free when admitting (a fit is admitted
+ * while free memory minus its need stays above this, or when the pool is
+ * empty). */
+int gbnuts_pool_create(int precision, int x_dtype, int max_fits, long long max_chains,
+                       long long reserve_bytes, gbnuts_pool** out);
+void gbnuts_pool_destroy(gbnuts_pool* p);
+
+/* Queues a fit: the model arguments of gbnuts_model_create and a run
+ * configuration (copied, with its inits / inv_metrics).  out's buffers must
+ * stay valid until the fit is done; they are written when it retires. */
+int gbnuts_pool_submit(gbnuts_pool* p, int kind, const void* X, int x_dtype, const double* y,
+                       const int* group, long long N, int K, int J, int intercept,
+                       const double* hp, int n_hp, const gbnuts_run_config* cfg,
+                       gbnuts_run_output* out, long long* fit_id);
+
+/* Admits queued fits (FIFO, while a slot, the chain budget and device
+ * memory allow), runs n_steps steps of all admitted fits, then retires the
+ * fits whose chains have all finished.  Reports fits running / queued. */
+int gbnuts_pool_step(gbnuts_pool* p, int n_steps, int* n_running, int* n_queued);
+
+/* state: 0 queued, 1 running, 2 done (*rc = the fit's return code, as
+ * gbnuts_sample_run's), 3 unknown id. */
+int gbnuts_pool_status(gbnuts_pool* p, long long fit_id, int* state, int* rc);
+
+/* Steps run so far and chains admitted now. */
+int gbnuts_pool_stats(gbnuts_pool* p, long long* steps, long long* chains);
+
 /* Device and build information: writes a short text description. */
 int gbnuts_device_info(char* buf, int cap);
 

@@ -99,6 +99,18 @@ SIGNATURES = {
         ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Callbacks)]),
     "gbnuts_sample_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RunConfig),
                                          ctypes.POINTER(RunOutput), ctypes.POINTER(Callbacks)]),
+    "gbnuts_pool_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_longlong, ctypes.c_longlong,
+                                          ctypes.POINTER(ctypes.c_void_p)]),
+    "gbnuts_pool_destroy": (None, [ctypes.c_void_p]),
+    "gbnuts_pool_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_int, _dp, _ip, ctypes.c_longlong,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp,
+                                          ctypes.c_int, ctypes.POINTER(RunConfig),
+                                          ctypes.POINTER(RunOutput), _llp]),
+    "gbnuts_pool_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _ip]),
+    "gbnuts_pool_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, _ip, _ip]),
+    "gbnuts_pool_stats": (ctypes.c_int, [ctypes.c_void_p, _llp, _llp]),
     "gbnuts_device_info": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "gbnuts_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
 }

@@ -22,6 +22,7 @@
 #include "../../include/gbnuts.h"
 #include "gbnuts_internal.h"
 #include "nuts_device.h"
+#include "capi_internal.h"
 
 namespace gbn {
 static thread_local std::string g_last_error;
@@ -30,28 +31,6 @@ const std::string& last_error() { return g_last_error; }
 }  // namespace gbn
 
 using namespace gbn;
-
-static int fail(int code, const std::string& msg) {
-  set_last_error(msg);
-  return code;
-}
-
-struct gbnuts_model {
-  ModelDesc desc;
-  void* d_X = nullptr;
-  double* d_y = nullptr;
-  int* d_group = nullptr;
-  std::vector<int> h_group_off;  // J+1
-  // single-point and batch scratch (owned by the handle)
-  GradWorkspace ws;
-  double* d_theta = nullptr;
-  double* d_lp = nullptr;
-  double* d_grad = nullptr;
-  int scratch_C = 0;
-  cudaStream_t stream = nullptr;
-  void* d_tc_xt = nullptr;
-  float* d_tc_yt = nullptr;
-};
 
 // Builds the tensor-core tiles of X on first use of the bf16x3 form.
 static int ensure_precision(gbnuts_model* m, int precision) {
@@ -441,15 +420,13 @@ struct DeviceRun {
 
 }  // namespace
 
-extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
-                                 gbnuts_run_output* out, const gbnuts_callbacks* cb) {
-  if (!m || !rc || !out) return fail(GBNUTS_USAGE, "bad arguments");
+int make_sampler_cfg(const gbnuts_model* m, const gbnuts_run_config* rc, int max_rows,
+                     int out_cols, SamplerCfg* cfg_out, std::vector<std::string>* messages) {
   const int C = rc->num_chains;
   const int D = m->desc.D;
   if (C <= 0) return fail(GBNUTS_USAGE, "num_chains must be positive");
   if (rc->num_warmup < 0 || rc->num_samples < 0) return fail(GBNUTS_USAGE, "negative iterations");
   if (rc->num_thin < 1) return fail(GBNUTS_USAGE, "num_thin must be at least 1");
-  if (!out->draws || !out->n_rows) return fail(GBNUTS_USAGE, "draws / n_rows buffers missing");
   // base_nuts::set_max_depth ignores non-positive depths (default 5)
   const int max_depth = rc->max_depth > 0 ? rc->max_depth : 5;
   if (max_depth > MAX_TREE_DEPTH) return fail(GBNUTS_USAGE, "max_depth above 16 is not supported");
@@ -462,10 +439,10 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   const int warm_rows = rc->save_warmup ? (rc->num_warmup + rc->num_thin - 1) / rc->num_thin : 0;
   const int samp_rows = (rc->num_samples + rc->num_thin - 1) / rc->num_thin;
   const int need_rows = warm_rows + samp_rows;
-  if (out->max_rows < need_rows || out->n_cols != n_cols)
+  if (max_rows < need_rows || out_cols != n_cols)
     return fail(GBNUTS_USAGE, "output buffer too small (max_rows / n_cols)");
 
-  SamplerCfg cfg;
+  SamplerCfg& cfg = *cfg_out;
   memset(&cfg, 0, sizeof(cfg));
   cfg.C = C;
   cfg.D = D;
@@ -477,7 +454,7 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   cfg.num_samples = rc->num_samples;
   cfg.num_thin = rc->num_thin;
   cfg.save_warmup = rc->save_warmup ? 1 : 0;
-  cfg.max_rows = out->max_rows;
+  cfg.max_rows = max_rows;
   cfg.n_cols = n_cols;
   cfg.stepsize = rc->stepsize > 0 ? rc->stepsize : 0.1;  // set_nominal_stepsize ignores e <= 0
   cfg.jitter = (rc->stepsize_jitter > 0 && rc->stepsize_jitter < 1) ? rc->stepsize_jitter : 0.0;
@@ -499,10 +476,29 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
     cfg.wa_base_window = wp.base_window;
     cfg.wa_size0 = wp.size0;
     cfg.wa_next0 = wp.next0;
-    if (cb && cb->log)
-      for (int c = 0; c < C; ++c)
-        for (auto& s : wp.messages) cb->log(cb->ctx, GBNUTS_INFO, s.c_str());
+    if (messages) *messages = wp.messages;
   }
+  return GBNUTS_OK;
+
+}
+
+extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
+                                 gbnuts_run_output* out, const gbnuts_callbacks* cb) {
+  if (!m || !rc || !out) return fail(GBNUTS_USAGE, "bad arguments");
+  if (!out->draws || !out->n_rows) return fail(GBNUTS_USAGE, "draws / n_rows buffers missing");
+  const int C = rc->num_chains;
+  const int D = m->desc.D;
+  const int n_cols = 7 + D;
+  SamplerCfg cfg;
+  std::vector<std::string> wmsg;
+  {
+    int r = make_sampler_cfg(m, rc, out->max_rows, out->n_cols, &cfg, &wmsg);
+    if (r) return r;
+  }
+  const int max_depth = cfg.max_depth;
+  if (cb && cb->log)
+    for (int c = 0; c < C; ++c)
+      for (auto& msg : wmsg) cb->log(cb->ctx, GBNUTS_INFO, msg.c_str());
 
   cudaStream_t st = m->stream;
   DeviceRun dr;
@@ -566,13 +562,59 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   GBN_CUDA_TRY(cudaEventRecord(ev_begin, st));
   auto wall0 = std::chrono::steady_clock::now();
 
+  // The step kernel and (for the fp64 / fp32 forms with up to 16 chains per
+  // block) the partial kernel run over one-entry fit tables: the same
+  // launches a pool makes, so the fit's draws equal its draws in any pool.
+  PoolFitDev h_fit;
+  h_fit.cfg = cfg;
+  h_fit.m = m->desc;
+  h_fit.f = FitPtrs{d_states, d_stacks, d_vecs, d_req, pv, d_active, d_draws,
+                    d_diag, d_init, d_inits, d_done, d_abort};
+  std::vector<int2> h_cmap(C);
+  for (int c = 0; c < C; ++c) h_cmap[c] = make_int2(0, c);
+  PoolFitDev* d_fit;
+  int2* d_cmap;
+  GBN_CUDA_TRY(dr.alloc(&d_fit, 1));
+  GBN_CUDA_TRY(dr.alloc(&d_cmap, C));
+  GBN_CUDA_TRY(cudaMemcpyAsync(d_fit, &h_fit, sizeof(h_fit), cudaMemcpyHostToDevice, st));
+  GBN_CUDA_TRY(cudaMemcpyAsync(d_cmap, h_cmap.data(), C * sizeof(int2), cudaMemcpyHostToDevice, st));
+  const bool pool_partials = rc->precision != GBNUTS_PREC_BF16X3 && chains_per_block(m->desc.K) == 16;
+  PoolGradFit* d_gfit = nullptr;
+  PoolWorkItem* d_items = nullptr;
+  int n_items = 0;
+  size_t pool_smem = 0;
+  if (pool_partials) {
+    const PoolGradFit g{m->desc, d_req, cfg.ld, C, d_active, m->ws.split_rows, m->ws.partial,
+                        m->ws.NP, m->ws.gz};
+    const int rb = partial_tile_rows(m->desc.K, rc->precision);
+    pool_smem = partial_smem(m->desc.K, rb, rc->precision);
+    std::vector<PoolWorkItem> items;
+    for (int s = 0; s < m->ws.S; ++s)
+      for (int b = 0; b < (C + 15) / 16; ++b) items.push_back(PoolWorkItem{0, s, b, rb});
+    n_items = (int)items.size();
+    GBN_CUDA_TRY(dr.alloc(&d_gfit, 1));
+    GBN_CUDA_TRY(dr.alloc(&d_items, items.size()));
+    GBN_CUDA_TRY(cudaMemcpyAsync(d_gfit, &g, sizeof(g), cudaMemcpyHostToDevice, st));
+    GBN_CUDA_TRY(cudaMemcpyAsync(d_items, items.data(), items.size() * sizeof(PoolWorkItem),
+                                 cudaMemcpyHostToDevice, st));
+    // the host tables must outlive the copies
+    GBN_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+
   // One step: every chain's state machine runs to its next gradient request,
   // then the gradient stage writes split partials the next step finalises.
   auto enqueue_step = [&](cudaEvent_t e0, cudaEvent_t e1) -> int {
-    launch_nuts_step(cfg, m->desc, d_states, d_stacks, d_vecs, d_req, pv, d_active, d_draws,
-                     d_diag, d_init, d_inits, d_done, d_abort, st);
-    return launch_partials(m->desc, rc->precision, d_req, cfg.ld, C, d_active, m->ws, st, e0,
-                           e1);
+    launch_nuts_step_pool(d_fit, d_cmap, C, st);
+    if (!pool_partials)
+      return launch_partials(m->desc, rc->precision, d_req, cfg.ld, C, d_active, m->ws, st, e0,
+                             e1);
+    if (m->desc.off_z >= 0)
+      GBN_CUDA_TRY(cudaMemsetAsync(m->ws.gz, 0, (size_t)C * m->desc.J * sizeof(double), st));
+    if (e0) cudaEventRecord(e0, st);
+    int r = launch_partials_pool(d_gfit, d_items, n_items, m->desc.x_dtype, rc->precision,
+                                 pool_smem, st);
+    if (e1) cudaEventRecord(e1, st);
+    return r;
   };
   // Steps run in chunks of 32 captured once into a CUDA graph; every 16th
   // chunk runs eagerly with CUDA events around the gradient kernel (its live

@@ -65,6 +65,10 @@ struct GradWorkspace {
   size_t bytes = 0;
 };
 
+// Row splits of a gradient launch for C chains (depends on the model and C
+// only, so a fit's sums are the same wherever it runs).
+int choose_splits(const ModelDesc& m, int C, int precision);
+
 // Chooses the split count and sets split row boundaries (group aligned for
 // hierarchical models).  Allocates (or reuses) the workspace.
 int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int precision,
@@ -83,6 +87,30 @@ int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int
                          int C, const int* active, double* lp, double* grad, int ldg,
                          int propto, int jacobian, GradWorkspace& ws,
                          cudaStream_t stream, cudaEvent_t ev0, cudaEvent_t ev1);
+
+// A fit's gradient stage inside a pool launch.
+struct PoolGradFit {
+  ModelDesc m;
+  const double* Q;
+  int ldq, C;
+  const int* active;
+  const long long* split_rows;
+  double* P;
+  int NP;
+  double* Gz;
+};
+// One CTA of a pool launch.
+struct PoolWorkItem {
+  int fit, split, chain_block, rb;
+};
+// Tile rows the partial kernel uses for a given K (same choice as a
+// single-fit launch, so a fit's sums do not depend on its pool neighbours).
+int partial_tile_rows(int K, int precision);
+size_t partial_smem(int K, int rb, int precision);
+// Launches the pool partial kernel for work items whose fits share x_dtype;
+// every fit must have chains_per_block(K) == 16.
+int launch_partials_pool(const PoolGradFit* d_fits, const PoolWorkItem* d_items, int n_items,
+                         int x_dtype, int precision, size_t smem, cudaStream_t st);
 
 // Maximum chains per block of the partial kernel for a given K (0 if K is
 // beyond what the kernel supports).

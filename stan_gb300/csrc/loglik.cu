@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <stdlib.h>
 
 #include "../../include/gbnuts.h"
 #include "gbnuts_internal.h"
@@ -81,12 +82,13 @@ __host__ __device__ inline size_t partial_smem_bytes(int CB, int K, int RB) {
          sizeof(int) * (size_t)RB;
 }
 
+// One CTA's work: split s of the rows, chain block cb (CB chains), RB rows per
+// shared-memory tile.
 template <typename XT, typename CT, int CB>
-__global__ void __launch_bounds__(kThreads)
-    loglik_partial_kernel(ModelDesc m, const double* __restrict__ Q, int ldq, int C,
-                          const int* __restrict__ active,
-                          const long long* __restrict__ split_rows, int RB,
-                          double* __restrict__ P, int NP, double* __restrict__ Gz) {
+__device__ __forceinline__ void loglik_partial_body(
+    const ModelDesc& m, const double* __restrict__ Q, int ldq, int C,
+    const int* __restrict__ active, const long long* __restrict__ split_rows, int RB,
+    double* __restrict__ P, int NP, double* __restrict__ Gz, int s, int cb) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int K = m.K;
   const int KP = K + 1;
@@ -100,8 +102,7 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ double red_s[kThreads][4];
 
   const int tid = threadIdx.x;
-  const int s = blockIdx.x;
-  const int c0 = blockIdx.y * CB;
+  const int c0 = cb * CB;
   const XT* __restrict__ X = static_cast<const XT*>(m.X);
 
   for (int idx = tid; idx < CB * K; idx += kThreads) {
@@ -280,6 +281,28 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+template <typename XT, typename CT, int CB>
+__global__ void __launch_bounds__(kThreads)
+    loglik_partial_kernel(ModelDesc m, const double* __restrict__ Q, int ldq, int C,
+                          const int* __restrict__ active,
+                          const long long* __restrict__ split_rows, int RB,
+                          double* __restrict__ P, int NP, double* __restrict__ Gz) {
+  loglik_partial_body<XT, CT, CB>(m, Q, ldq, C, active, split_rows, RB, P, NP, Gz, blockIdx.x,
+                                  blockIdx.y);
+}
+
+// Many fits in one launch: CTA b runs work item items[b] (fit, split, chain
+// block, tile rows), each fit with its own data and partial buffers.
+template <typename XT, typename CT, int CB>
+__global__ void __launch_bounds__(kThreads)
+    loglik_partial_pool_kernel(const PoolGradFit* __restrict__ fits,
+                               const PoolWorkItem* __restrict__ items) {
+  const PoolWorkItem it = items[blockIdx.x];
+  const PoolGradFit& f = fits[it.fit];
+  loglik_partial_body<XT, CT, CB>(f.m, f.Q, f.ldq, f.C, f.active, f.split_rows, it.rb, f.P,
+                                  f.NP, f.Gz, it.split, it.chain_block);
+}
+
 // Per chain (one warp): split sums + priors + Jacobians -> lp, grad.
 __global__ void __launch_bounds__(128)
     loglik_finalize_kernel(ModelDesc m, const double* __restrict__ Q, int ldq, int C,
@@ -287,12 +310,14 @@ __global__ void __launch_bounds__(128)
                            int NP, int S, const double* __restrict__ Gz,
                            double* __restrict__ lp_out, double* __restrict__ grad, int ldg,
                            int propto, int jacobian) {
+  __shared__ double sh_cs[4][kMaxColSums];
   const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (c >= C) return;
+  if (c >= C) return;  // uniform per warp
   if (active && !active[c]) return;
   const double lp = finalize_chain(m, Q + (size_t)c * ldq, c, C, P, NP, S, Gz,
-                                   grad + (size_t)c * ldg, 1.0, propto, jacobian, lane);
+                                   grad + (size_t)c * ldg, 1.0, propto, jacobian, lane,
+                                   sh_cs[threadIdx.x >> 5]);
   if (lane == 0) lp_out[c] = lp;
 }
 
@@ -351,6 +376,69 @@ static void dispatch_x(const ModelDesc& m, const double* Q, int ldq, int C,
     dispatch_cb<uint16_t, CT>(m, Q, ldq, C, active, ws, st);
 }
 
+int partial_tile_rows(int K, int precision) {
+  const int CB = chains_per_block(K);
+  return precision == GBNUTS_PREC_FP64 ? choose_rb<double>(CB, K) : choose_rb<float>(CB, K);
+}
+
+size_t partial_smem(int K, int rb, int precision) {
+  const int CB = chains_per_block(K);
+  return precision == GBNUTS_PREC_FP64 ? partial_smem_bytes<double>(CB, K, rb)
+                                       : partial_smem_bytes<float>(CB, K, rb);
+}
+
+template <typename XT, typename CT>
+static int launch_pool_t(const PoolGradFit* d_fits, const PoolWorkItem* d_items, int n_items,
+                         size_t smem, cudaStream_t st) {
+  static size_t done = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    if (smem > done) {
+      GBN_CUDA_TRY(cudaFuncSetAttribute(loglik_partial_pool_kernel<XT, CT, 16>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      done = smem;
+    }
+  }
+  loglik_partial_pool_kernel<XT, CT, 16><<<n_items, kThreads, smem, st>>>(d_fits, d_items);
+  GBN_CUDA_TRY(cudaGetLastError());
+  return GBNUTS_OK;
+}
+
+int launch_partials_pool(const PoolGradFit* d_fits, const PoolWorkItem* d_items, int n_items,
+                         int x_dtype, int precision, size_t smem, cudaStream_t st) {
+  if (n_items <= 0) return GBNUTS_OK;
+  const bool f64 = precision == GBNUTS_PREC_FP64;
+  if (x_dtype == GBNUTS_F64)
+    return f64 ? launch_pool_t<double, double>(d_fits, d_items, n_items, smem, st)
+               : launch_pool_t<double, float>(d_fits, d_items, n_items, smem, st);
+  if (x_dtype == GBNUTS_F32)
+    return f64 ? launch_pool_t<float, double>(d_fits, d_items, n_items, smem, st)
+               : launch_pool_t<float, float>(d_fits, d_items, n_items, smem, st);
+  return f64 ? launch_pool_t<uint16_t, double>(d_fits, d_items, n_items, smem, st)
+             : launch_pool_t<uint16_t, float>(d_fits, d_items, n_items, smem, st);
+}
+
+// Minimum rows of a split (GBNUTS_SPLIT_ROWS overrides it, for tuning).
+static long long split_rows_min() {
+  static const long long v = [] {
+    const char* e = getenv("GBNUTS_SPLIT_ROWS");
+    const long long r = e ? atoll(e) : 0;
+    return r > 0 ? r : 64LL;
+  }();
+  return v;
+}
+
+int choose_splits(const ModelDesc& m, int C, int precision) {
+  if (precision == GBNUTS_PREC_BF16X3) return tc_splits(m, C);
+  const int CB = chains_per_block(m.K);
+  const int chain_blocks = (C + CB - 1) / CB;
+  // Splits: enough CTAs for ~2 waves over 152 SMs, a minimum of rows each.
+  long long max_s = std::max(1LL, m.N / split_rows_min());
+  int S = (int)std::min<long long>(max_s, std::max(1, (2 * 152 + chain_blocks - 1) / chain_blocks));
+  if (m.off_z >= 0) S = std::min(S, m.J);
+  return std::max(S, 1);
+}
+
 int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int precision,
                       GradWorkspace& ws) {
   const int CB = chains_per_block(m.K);
@@ -358,21 +446,11 @@ int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int pre
     set_last_error("K beyond the supported maximum (2048)");
     return GBNUTS_USAGE;
   }
-  int S;
-  if (precision == GBNUTS_PREC_BF16X3) {
-    if (!tc_supported(m)) {
-      set_last_error("bf16x3 precision needs a logistic or Poisson GLM with K + intercept <= 128");
-      return GBNUTS_USAGE;
-    }
-    S = tc_splits(m, C);
-  } else {
-    const int chain_blocks = (C + CB - 1) / CB;
-    // Splits: enough CTAs for ~2 waves over 152 SMs, at least 64 rows each.
-    long long max_s = std::max(1LL, m.N / 64);
-    S = (int)std::min<long long>(max_s, std::max(1, (2 * 152 + chain_blocks - 1) / chain_blocks));
-    if (m.off_z >= 0) S = std::min(S, m.J);
-    S = std::max(S, 1);
+  if (precision == GBNUTS_PREC_BF16X3 && !tc_supported(m)) {
+    set_last_error("bf16x3 precision needs a logistic or Poisson GLM with K + intercept <= 128");
+    return GBNUTS_USAGE;
   }
+  const int S = choose_splits(m, C, precision);
   const int NP = n_partials(m);
   size_t need = (size_t)S * C * NP * sizeof(double) +
                 (m.off_z >= 0 ? (size_t)C * m.J * sizeof(double) : 0) +

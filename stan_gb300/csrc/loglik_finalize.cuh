@@ -1,7 +1,9 @@
 // Finalisation of one chain's log density and gradient from the split
-// partial sums: split sums in split order (deterministic), priors, the
+// partial sums: split sums in a fixed order (deterministic), priors, the
 // Jacobian of tau = exp(u), sigma = exp(u), and the chain rule through them.
 // One warp per chain, lanes over the coordinates; returns lp in every lane.
+// With many splits the split sums run with lanes over splits (a butterfly per
+// column) into a shared buffer, else with lanes over columns in split order.
 // Shared by the batched-gradient finalize kernel and the sampler step kernel.
 #pragma once
 
@@ -13,14 +15,46 @@ namespace gbn {
 
 static constexpr double kLogSqrt2Pi = 0.91893853320467274178032973640562;
 
-// th: the chain's parameters; grad_out[d] = sign * d lp / d theta_d.
+// Largest partial count whose split sums go through the warp's shared buffer.
+static constexpr int kMaxColSums = 4 + 512;
+// Splits from which the sums run with lanes over splits instead of columns.
+static constexpr int kLanesOverSplits = 32;
+
+// Column sums over the S splits of one chain's partials (row stride pstride),
+// lanes over splits, a fixed butterfly per column: cs[k] for k < NP.  The
+// order of additions depends on S and NP only.
+__device__ __forceinline__ void split_column_sums(const double* __restrict__ Pc, size_t pstride,
+                                                  int S, int NP, double* cs, int lane) {
+#pragma unroll 4
+  for (int k = 0; k < NP; ++k) {
+    double a = 0;
+    for (int s = lane; s < S; s += 32) a += Pc[s * pstride + k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+    if (lane == 0) cs[k] = a;
+  }
+  __syncwarp();
+}
+
+// th: the chain's parameters; grad_out[d] = sign * d lp / d theta_d.  cs: the
+// warp's shared buffer of kMaxColSums doubles.
 __device__ __forceinline__ double finalize_chain(const ModelDesc& m, const double* th, int c,
                                                  int C, const double* __restrict__ P, int NP,
                                                  int S, const double* __restrict__ Gz,
                                                  double* grad_out, double sign, int propto,
-                                                 int jacobian, int lane) {
+                                                 int jacobian, int lane, double* cs) {
   const size_t pstride = (size_t)C * NP;
   const double* Pc = P + (size_t)c * NP;
+  const bool use_cs = S >= kLanesOverSplits && NP <= kMaxColSums;
+  if (use_cs) split_column_sums(Pc, pstride, S, NP, cs, lane);
+  // sum over splits of partial column k (split order when lanes run over columns)
+  auto col = [&](int k) -> double {
+    if (use_cs) return cs[k];
+    double a = 0;
+#pragma unroll 4
+    for (int s = 0; s < S; ++s) a += Pc[s * pstride + k];
+    return a;
+  };
   const double tau = m.idx_tau >= 0 ? exp(th[m.idx_tau]) : 0.0;
   const double jac = jacobian ? 1.0 : 0.0;
   double prior = 0.0;
@@ -29,30 +63,26 @@ __device__ __forceinline__ double finalize_chain(const ModelDesc& m, const doubl
     double g;
     if (d >= m.off_beta) {
       const int k = d - m.off_beta;
-      double sum = 0;
-      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 4 + k];
+      const double sum = col(4 + k);
       g = sum - t / (m.s_beta * m.s_beta);
       const double z = t / m.s_beta;
       prior += -0.5 * z * z;
       if (!propto) prior += -log(m.s_beta) - kLogSqrt2Pi;
     } else if (d == 0 && m.has_base) {
-      double sum = 0;
-      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 1];
+      const double sum = col(1);
       g = sum - t / (m.s_base * m.s_base);
       const double z = t / m.s_base;
       prior += -0.5 * z * z;
       if (!propto) prior += -log(m.s_base) - kLogSqrt2Pi;
     } else if (d == m.idx_tau) {
-      double sum = 0;
-      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 2];
+      const double sum = col(2);
       g = tau * (sum - tau / (m.s_tau * m.s_tau)) + jac;
       const double z = tau / m.s_tau;
       prior += -0.5 * z * z + jac * t;
       if (!propto) prior += -log(m.s_tau) - kLogSqrt2Pi;
     } else if (d == m.idx_sigma) {
       const double sigma = exp(t);
-      double sum = 0;
-      for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 3];
+      const double sum = col(3);
       const double dsig = -(double)m.N / sigma + sum / (sigma * sigma * sigma) -
                           sigma / (m.s_sigma * m.s_sigma);
       g = sigma * dsig + jac;
@@ -69,9 +99,7 @@ __device__ __forceinline__ double finalize_chain(const ModelDesc& m, const doubl
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) prior += __shfl_xor_sync(0xffffffffu, prior, off);
-  double sum = 0;
-  for (int s = 0; s < S; ++s) sum += Pc[s * pstride + 0];
-  double lp = sum + prior;
+  double lp = col(0) + prior;
   if (!propto) {
     if (m.link == LINK_NORMAL) lp += -(double)m.N * kLogSqrt2Pi;
     if (m.link == LINK_POISSON_LOG) lp += -m.sum_lgamma_y;

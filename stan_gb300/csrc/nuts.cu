@@ -402,33 +402,37 @@ static __device__ void finish_chain(ChainState& st, int status, int* done_count,
   if (lane == 0) atomicAdd(done_count, 1);
 }
 
-__global__ void __launch_bounds__(128)
-    nuts_step_kernel(SamplerCfg cfg, ModelDesc m, ChainState* __restrict__ states,
-                     ChainStack* __restrict__ stacks, double* vecs, double* __restrict__ req,
-                     PartialsView pv, int* __restrict__ active, double* __restrict__ draws,
-                     double* __restrict__ diag, double* __restrict__ init_out,
-                     const double* __restrict__ inits, int* __restrict__ done_count,
-                     const int* __restrict__ abort_flag) {
-  __shared__ double sh_lsw[4][MAX_TREE_DEPTH];
-  __shared__ double sh_V[4][MAX_TREE_DEPTH];
-  __shared__ int sh_slot[4][MAX_TREE_DEPTH];
-  const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  const int wl = threadIdx.x >> 5;
-  if (c >= cfg.C) return;
+// One chain's step: runs its state machine from where it yielded to its next
+// gradient request (or to the end of its run).  Called by a whole warp.
+static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, const ModelDesc& m,
+                                                       const FitPtrs& f, int c, int lane,
+                                                       double* lsw_s, double* V_s, int* slot_s,
+                                                       double* cs_s) {
+  ChainState* __restrict__ states = f.states;
+  ChainStack* __restrict__ stacks = f.stacks;
+  double* vecs = f.vecs;
+  double* __restrict__ req = f.req;
+  const PartialsView pv = f.pv;
+  int* __restrict__ active = f.active;
+  double* __restrict__ draws = f.draws;
+  double* __restrict__ diag = f.diag;
+  double* __restrict__ init_out = f.init_out;
+  const double* __restrict__ inits = f.inits;
+  int* __restrict__ done_count = f.done_count;
+  const int* __restrict__ abort_flag = f.abort_flag;
   ChainState st = states[c];
   if (st.done) {
     if (lane == 0) active[c] = 0;
     return;
   }
   if (lane < MAX_TREE_DEPTH) {
-    sh_lsw[wl][lane] = stacks[c].lsw[lane];
-    sh_slot[wl][lane] = stacks[c].slot[lane];
+    lsw_s[lane] = stacks[c].lsw[lane];
+    slot_s[lane] = stacks[c].slot[lane];
   } else {
-    sh_V[wl][lane - MAX_TREE_DEPTH] = stacks[c].V[lane - MAX_TREE_DEPTH];
+    V_s[lane - MAX_TREE_DEPTH] = stacks[c].V[lane - MAX_TREE_DEPTH];
   }
   __syncwarp();
-  const Stk sk{sh_lsw[wl], sh_V[wl], sh_slot[wl]};
+  const Stk sk{lsw_s, V_s, slot_s};
   Ctx x{cfg, vecs, c, lane};
   const int D = cfg.D;
   double* rq = req + (size_t)c * cfg.ld;
@@ -440,7 +444,7 @@ __global__ void __launch_bounds__(128)
   // partials into the working point's g slot (g = -grad lp); returns V.
   auto resume = [&](int q_slot, int g_slot) -> double {
     const double lp = finalize_chain(m, x.slot(q_slot), c, cfg.C, pv.P, pv.NP, pv.S, pv.Gz,
-                                     x.slot(g_slot), -1.0, 1, 1, lane);
+                                     x.slot(g_slot), -1.0, 1, 1, lane, cs_s);
     if (isnan(lp)) return lp;
     if (!isfinite(lp)) return inf;
     return -lp;
@@ -819,6 +823,32 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// Chains of one or many fits in one launch: warp g runs chain chain_map[g].y
+// of fit chain_map[g].x.  A single-fit run launches the same kernel with a
+// one-entry table, so a fit's arithmetic is the same compiled code alone and
+// in a pool.  Each warp first copies its fit's descriptor to shared memory.
+__global__ void __launch_bounds__(128, 1)
+    nuts_step_pool_kernel(const PoolFitDev* __restrict__ fits, const int2* __restrict__ chain_map,
+                          int total) {
+  __shared__ double sh_lsw[4][MAX_TREE_DEPTH];
+  __shared__ double sh_V[4][MAX_TREE_DEPTH];
+  __shared__ int sh_slot[4][MAX_TREE_DEPTH];
+  __shared__ double sh_cs[4][kMaxColSums];
+  __shared__ PoolFitDev sh_fit[4];
+  static_assert(sizeof(PoolFitDev) % 8 == 0, "descriptor copied as 8-byte words");
+  const int g = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  const int wl = threadIdx.x >> 5;
+  if (g >= total) return;  // uniform per warp
+  const int2 fc = chain_map[g];
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(fits + fc.x);
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sh_fit[wl]);
+  for (int i = lane; i < (int)(sizeof(PoolFitDev) / 8); i += 32) dst[i] = src[i];
+  __syncwarp();
+  const PoolFitDev& pf = sh_fit[wl];
+  nuts_step_chain(pf.cfg, pf.m, pf.f, fc.y, lane, sh_lsw[wl], sh_V[wl], sh_slot[wl], sh_cs[wl]);
+}
+
 // Sets every chain's state from the configuration (service set-up,
 // hmc_nuts_diag_e_adapt.hpp:360-381).
 __global__ void nuts_init_kernel(SamplerCfg cfg, ChainState* states, ChainStack* stacks,
@@ -866,16 +896,12 @@ void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* sta
   nuts_init_kernel<<<blocks, threads, 0, s>>>(cfg, states, stacks, vecs, inv_metrics, active);
 }
 
-void launch_nuts_step(const SamplerCfg& cfg, const ModelDesc& m, ChainState* states,
-                      ChainStack* stacks, double* vecs, double* req, PartialsView pv,
-                      int* active, double* draws, double* diag, double* init_out,
-                      const double* inits, int* done_count, const int* abort_flag,
-                      cudaStream_t s) {
+void launch_nuts_step_pool(const PoolFitDev* fits, const int2* chain_map, int total,
+                           cudaStream_t s) {
+  if (total <= 0) return;
   const int threads = 128;
-  const int blocks = (int)(((size_t)cfg.C * 32 + threads - 1) / threads);
-  nuts_step_kernel<<<blocks, threads, 0, s>>>(cfg, m, states, stacks, vecs, req, pv, active,
-                                              draws, diag, init_out, inits, done_count,
-                                              abort_flag);
+  const int blocks = (int)(((size_t)total * 32 + threads - 1) / threads);
+  nuts_step_pool_kernel<<<blocks, threads, 0, s>>>(fits, chain_map, total);
 }
 
 }  // namespace gbn

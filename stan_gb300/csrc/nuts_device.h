@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "gbnuts_internal.h"
+
 namespace gbn {
 
 constexpr int MAX_TREE_DEPTH = 16;
@@ -66,7 +68,6 @@ struct ChainStack {
   int slot[MAX_TREE_DEPTH];
 };
 
-struct ModelDesc;
 
 // Where the step kernel finds the gradient stage's split partial sums.
 struct PartialsView {
@@ -75,12 +76,35 @@ struct PartialsView {
   const double* Gz;
 };
 
+// Device pointers of one fit's sampler state and gradient stage.
+struct FitPtrs {
+  ChainState* states;
+  ChainStack* stacks;
+  double* vecs;
+  double* req;  // positions whose gradient the chains request, [C][ld]
+  PartialsView pv;
+  int* active;
+  double* draws;
+  double* diag;
+  double* init_out;
+  const double* inits;
+  int* done_count;
+  const int* abort_flag;
+};
+
 void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* stacks,
                       double* vecs, const double* inv_metrics, int* active, cudaStream_t s);
-void launch_nuts_step(const SamplerCfg& cfg, const ModelDesc& m, ChainState* states,
-                      ChainStack* stacks, double* vecs, double* req, PartialsView pv,
-                      int* active, double* draws, double* diag, double* init_out,
-                      const double* inits, int* done_count, const int* abort_flag,
-                      cudaStream_t s);
+
+// A fit as the step kernel sees it (device-resident table entry).  Single-fit
+// runs and pools both launch the step kernel over a table of these.
+struct PoolFitDev {
+  SamplerCfg cfg;
+  ModelDesc m;
+  FitPtrs f;
+};
+
+// One step of `total` chains: chain_map[g] = (table index, chain in fit).
+void launch_nuts_step_pool(const PoolFitDev* fits, const int2* chain_map, int total,
+                           cudaStream_t s);
 
 }  // namespace gbn

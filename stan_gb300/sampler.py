@@ -39,13 +39,17 @@ class RunResult:
         return np.transpose(self.draws[:, w:n], (1, 0, 2))
 
 
-def run(model, num_chains=4, adapt=True, num_warmup=1000, num_samples=1000, num_thin=1,
-        save_warmup=False, stepsize=1.0, stepsize_jitter=0.0, max_depth=10, delta=0.8,
-        gamma=0.05, kappa=0.75, t0=10.0, init_buffer=75, term_buffer=50, window=25,
-        init_radius=2.0, random_seed=0, init_chain_id=1, precision="fp64",
-        inits=None, inv_metrics=None, save_diagnostics=False):
-    lib = _lib.load()
-    C, D = num_chains, model.D
+def prepare(D, num_chains=4, adapt=True, num_warmup=1000, num_samples=1000, num_thin=1,
+            save_warmup=False, stepsize=1.0, stepsize_jitter=0.0, max_depth=10, delta=0.8,
+            gamma=0.05, kappa=0.75, t0=10.0, init_buffer=75, term_buffer=50, window=25,
+            init_radius=2.0, random_seed=0, init_chain_id=1, precision="fp64",
+            inits=None, inv_metrics=None, save_diagnostics=False):
+    """Run configuration and caller-owned output buffers for a fit of dimension D.
+
+    Returns (config, output, result): the ctypes structures point into the
+    arrays of `result`, which must stay alive until the run has written them.
+    """
+    C = num_chains
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
     ini = None if inits is None else np.ascontiguousarray(inits, dtype=np.float64).reshape(C, D)
     imi = None if inv_metrics is None else np.ascontiguousarray(inv_metrics, dtype=np.float64).reshape(C, D)
@@ -58,24 +62,33 @@ def run(model, num_chains=4, adapt=True, num_warmup=1000, num_samples=1000, num_
         (num_samples + num_thin - 1) // num_thin
     rows = max(rows, 1)
     ncol = 7 + D
-    draws = np.zeros((C, rows, ncol))
-    diag = np.zeros((C, rows, 3 * D)) if save_diagnostics else None
-    n_rows = np.zeros(C, dtype=np.int32)
-    n_warm = np.zeros(C, dtype=np.int32)
-    status = np.zeros(C, dtype=np.int32)
-    eps = np.zeros(C)
-    invm = np.zeros((C, D))
-    init = np.zeros((C, D))
-    ngrad = np.zeros(C, dtype=np.int64)
-    secs = np.zeros((C, 2))
-    out = _lib.RunOutput(rows, ncol, _ptr(draws), None if diag is None else _ptr(diag),
-                         n_rows.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
-                         n_warm.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
-                         status.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
-                         _ptr(eps), _ptr(invm), _ptr(init),
-                         ngrad.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), _ptr(secs),
-                         0.0, 0.0, 0, 0)
+    res = RunResult(np.zeros((C, rows, ncol)), np.zeros(C, dtype=np.int32),
+                    np.zeros(C, dtype=np.int32), np.zeros(C, dtype=np.int32), np.zeros(C),
+                    np.zeros((C, D)), np.zeros((C, D)), np.zeros(C, dtype=np.int64),
+                    np.zeros((C, 2)), 0.0, 0.0, 0, 0,
+                    np.zeros((C, rows, 3 * D)) if save_diagnostics else None)
+    res._keep = (ini, imi)
+    ip = ctypes.POINTER(ctypes.c_int)
+    out = _lib.RunOutput(rows, ncol, _ptr(res.draws),
+                         None if res.diagnostics is None else _ptr(res.diagnostics),
+                         res.n_rows.ctypes.data_as(ip), res.n_warmup_rows.ctypes.data_as(ip),
+                         res.status.ctypes.data_as(ip), _ptr(res.stepsize), _ptr(res.inv_metric),
+                         _ptr(res.init), res.n_grad.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                         _ptr(res.seconds), 0.0, 0.0, 0, 0)
+    return cfg, out, res
+
+
+def finish(out, res):
+    """Copies the run totals of `out` into `res`."""
+    res.total_ms, res.grad_ms = out.total_ms, out.grad_ms
+    res.steps, res.kernel_launches = out.steps, out.kernel_launches
+    return res
+
+
+def run(model, num_chains=4, **kwargs):
+    """One fit through gbnuts_sample_run (the keyword arguments of prepare())."""
+    lib = _lib.load()
+    cfg, out, res = prepare(model.D, num_chains, **kwargs)
     rc = lib.gbnuts_sample_run(model.handle, ctypes.byref(cfg), ctypes.byref(out), None)
     _lib.check(rc, "gbnuts_sample_run")
-    return RunResult(draws, n_rows, n_warm, status, eps, invm, init, ngrad, secs,
-                     out.total_ms, out.grad_ms, out.steps, out.kernel_launches, diag)
+    return finish(out, res)
