@@ -17,6 +17,13 @@ extern "C" {
 int gbnuts_tc_probe(const uint16_t* A, const uint16_t* B, const uint16_t* R, float* D1,
                     float* D2);
 
+/* The chains-on-M layouts: D1 = A . X^T and D2 = R . X with A and R held in
+ * tensor memory (128 lanes x 64 32-bit words each, Aw / Rw, written as given:
+ * two bf16 per word) and X a 128x128 bf16 matrix (row-major uint16 bit
+ * patterns); D1, D2 128x128 fp32 outputs.  Returns 0 on success. */
+int gbnuts_tct_probe(const uint32_t* Aw, const uint16_t* X, const uint32_t* Rw, float* D1,
+                     float* D2);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,6 +122,13 @@ int tc_splits(const ModelDesc& m, int C);
 int tc_prepare(const ModelDesc& m, void** xt, float** yt, int* n_tiles, cudaStream_t st);
 int launch_tc(const ModelDesc& m, const double* Q, int ldq, int C, const int* active,
               GradWorkspace& ws, cudaStream_t st);
+// Chains-on-M form (Theta and R as tensor-memory operands, 128 chains per CTA).
+int tct_splits(const ModelDesc& m, int C);
+int launch_tct(const ModelDesc& m, const double* Q, int ldq, int C, const int* active,
+               GradWorkspace& ws, cudaStream_t st);
+// Which tensor-core kernel the bf16x3 form uses (GBNUTS_TC_KERNEL=m64 selects
+// the chains-on-N kernel, for comparisons).
+bool tc_chains_on_m();
 // Whether the model can use the tensor-core form.
 inline bool tc_supported(const ModelDesc& m) {
   return (m.link == LINK_LOGIT || m.link == LINK_POISSON_LOG) && m.off_z < 0 &&

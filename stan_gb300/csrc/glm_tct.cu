@@ -1,0 +1,522 @@
+// Batched GLM log density and gradient on the tcgen05 tensor cores, chains on
+// the M dimension (precision GBNUTS_PREC_BF16X3, logistic and Poisson).
+//
+// A CTA owns 128 chains (one per TMEM lane) and a range of 128-row tiles of X,
+// taken 64 rows at a time:
+//   GEMM1  eta^T (128 chains x 64 rows)  = Theta . X_half^T      A = Theta in TMEM
+//   link   term, r = d lp / d eta        per (chain, row), fp32, read from TMEM
+//   GEMM2  G^T (128 chains x 128 feats) += R . X_half             A = R in TMEM
+// Theta and R are A operands held in tensor memory (bf16 hi and lo parts,
+// two elements per 32-bit column), so every MMA reads only its X operand
+// from shared memory: GEMM1 reads X K-major (rows x features) and GEMM2 the
+// same bytes MN-major (features x rows).  X, Theta and R are each split into
+// bf16 hi + lo and the three products hi.hi + hi.lo + lo.hi accumulate in
+// fp32 (x has no lo part when stored in bf16).  Each epilogue thread owns one
+// chain, so the lp sum over rows stays in the thread.
+//
+// TMEM columns (512): eta^T double buffer [0, 128), G^T [128, 256), Theta hi
+// [256, 320) and lo [320, 384), R double buffer [384, 512) (hi 32 + lo 32
+// columns per 64 rows).  Shared memory: a 3-stage ring of 128-row X tiles
+// (hi + lo + y, 65 KiB each).
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include <algorithm>
+
+#include "../../include/gbnuts.h"
+#include "gbnuts_internal.h"
+#include "tc_common.cuh"
+
+namespace gbn {
+
+using namespace tc;
+
+namespace tct {
+
+constexpr int TM = 128;            // rows per pre-tiled X tile
+constexpr int HR = 64;             // rows per GEMM1 / epilogue / GEMM2 pass
+constexpr int TK = 128;            // features per tile (K + intercept, zero padded)
+constexpr int NCH = 128;           // chains per CTA (TMEM lanes)
+constexpr int PART_BYTES = TM * TK * 2;   // one bf16 part of an X tile
+constexpr int HALF_BYTES = HR * TK * 2;   // rows [64h, 64h+64) of a part
+constexpr int Y_BYTES = TM * 4;
+constexpr int STAGE_BYTES = 2 * PART_BYTES + 1024;  // X hi, X lo, y (padded)
+constexpr int STAGES = 3;
+constexpr int NUM_EPI_WARPS = 8;   // two per TMEM lane quarter
+constexpr int THREADS = 64 + 32 * NUM_EPI_WARPS;
+constexpr int SMEM_X = 0;
+constexpr int SMEM_LP = SMEM_X + STAGES * STAGE_BYTES;   // [2][NCH] doubles
+constexpr int SMEM_BAR = SMEM_LP + 2 * NCH * 8;
+constexpr int SMEM_TOTAL = SMEM_BAR + 256;
+constexpr int SMEM_ALLOC = SMEM_TOTAL + 1024;  // slack for 1 KiB alignment
+// TMEM column map
+constexpr uint32_t COL_D1 = 0, COL_D2 = 128, COL_TH = 256, COL_TL = 320, COL_R = 384;
+
+// GEMM1 B operand: rows [64h, 64h+64) of a K-major tile part, features ks*16.
+__device__ __forceinline__ uint64_t desc_rows(uint32_t part, int h, int ks) {
+  return make_desc(part + h * HALF_BYTES + 256 * ks, 128, (TK / 8) * 128);
+}
+// GEMM2 B operand: the same part read MN-major (features x rows), rows
+// 64h + 16ks .. +16.
+__device__ __forceinline__ uint64_t desc_feats(uint32_t part, int h, int ks) {
+  return make_desc(part + h * HALF_BYTES + 4096 * ks, (TK / 8) * 128, 128);
+}
+
+}  // namespace tct
+
+struct TctArgs {
+  const __nv_bfloat16* xt;  // pre-tiled X (hi/lo per 128-row tile)
+  const float* yt;          // y per tile row
+  long long N;
+  int K, has_base, n_tiles;
+  const double* Q;
+  int ldq, C;
+  const int* active;
+  double* P;
+  int NP, S;
+  int* err;
+};
+
+namespace tct {
+// barrier slots (uint64 each) inside SMEM_BAR
+enum { B_XFULL = 0, B_XEMPTY = 3, B_D1FULL = 6, B_D1EMPTY = 8, B_RFULL = 10, B_REMPTY = 12,
+       B_D2FULL = 14, B_THETA = 15, B_COUNT = 16 };
+}  // namespace tct
+
+template <int LINK, bool XLO>
+__global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
+  using namespace tct;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  double* sLP = reinterpret_cast<double*>(sm + SMEM_LP);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + SMEM_BAR);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + SMEM_BAR + 8 * B_COUNT);
+  volatile int* abort_s = reinterpret_cast<volatile int*>(sm + SMEM_BAR + 8 * B_COUNT + 8);
+  __shared__ int act_s[NCH];
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int s = blockIdx.x;
+  const int c0 = blockIdx.y * NCH;
+  const int hb = a.has_base;
+  const int Kx = a.K + hb;
+
+  if (tid < NCH) {
+    const int cg = c0 + tid;
+    act_s[tid] = (cg < a.C) && (a.active == nullptr || a.active[cg] != 0);
+  }
+  const int any = __syncthreads_or(tid < NCH ? act_s[tid] : 0);
+  if (!any) return;
+
+  if (tid == 0) {
+    for (int b = 0; b < STAGES; ++b) {
+      mbar_init(&bars[B_XFULL + b], 1);
+      mbar_init(&bars[B_XEMPTY + b], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&bars[B_D1FULL + b], 1);
+      mbar_init(&bars[B_D1EMPTY + b], NUM_EPI_WARPS);
+      mbar_init(&bars[B_RFULL + b], NUM_EPI_WARPS);
+      mbar_init(&bars[B_REMPTY + b], 1);
+    }
+    mbar_init(&bars[B_D2FULL], 1);
+    mbar_init(&bars[B_THETA], NUM_EPI_WARPS);
+    *abort_s = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, 512);
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  const int t_begin = (int)((long long)a.n_tiles * s / a.S);
+  const int t_end = (int)((long long)a.n_tiles * (s + 1) / a.S);
+  const int n = t_end - t_begin;
+  const int passes = 2 * n;
+  const uint32_t x_bytes = XLO ? 2u * PART_BYTES : (uint32_t)PART_BYTES;
+
+  if (n > 0) {
+    if (warp == 0) {
+      // ---- producer: X tiles through the 3-stage ring
+      if (lane == 0) {
+        for (int i = 0; i < n; ++i) {
+          const int st = i % STAGES, u = i / STAGES;
+          if (!mbar_wait_abortable(&bars[B_XEMPTY + st], (u & 1) ^ 1, abort_s, a.err, 21)) break;
+          unsigned char* dst = sm + SMEM_X + st * STAGE_BYTES;
+          const __nv_bfloat16* src = a.xt + (size_t)(2 * (t_begin + i)) * (TM * TK);
+          mbar_arrive_expect_tx(&bars[B_XFULL + st], x_bytes + Y_BYTES);
+          bulk_copy_g2s(dst, src, PART_BYTES, &bars[B_XFULL + st]);
+          if (XLO)
+            bulk_copy_g2s(dst + PART_BYTES, src + TM * TK, PART_BYTES, &bars[B_XFULL + st]);
+          bulk_copy_g2s(dst + 2 * PART_BYTES, a.yt + (size_t)(t_begin + i) * TM, Y_BYTES,
+                        &bars[B_XFULL + st]);
+        }
+      }
+      __syncwarp();
+    } else if (warp == 1) {
+      // ---- MMA issuer: GEMM1 of pass p, then GEMM2 of pass p - 1
+      if (lane == 0) {
+        const uint32_t id1 = make_idesc_bf16(NCH, HR, 0, 0);
+        const uint32_t id2 = make_idesc_bf16(NCH, TK, 0, 1);
+        bool ok = mbar_wait_abortable(&bars[B_THETA], 0, abort_s, a.err, 22);
+        fence_after_sync();
+        auto gemm2 = [&](int p) -> bool {
+          const int b = p & 1;
+          if (!mbar_wait_abortable(&bars[B_RFULL + b], (p >> 1) & 1, abort_s, a.err, 23))
+            return false;
+          fence_after_sync();
+          const int i = p >> 1, h = p & 1, st = i % STAGES;
+          const uint32_t xh = smem_u32(sm + SMEM_X + st * STAGE_BYTES);
+          const uint32_t xl = xh + PART_BYTES;
+          const uint32_t rh = tmem + COL_R + 64 * b, rl = rh + 32;
+#pragma unroll 1
+          for (int ks = 0; ks < HR / 16; ++ks) {
+            const uint64_t bh = desc_feats(xh, h, ks);
+            mma_bf16_tmem_a(tmem + COL_D2, rh + 8 * ks, bh, id2, (p > 0 || ks > 0) ? 1u : 0u);
+            mma_bf16_tmem_a(tmem + COL_D2, rl + 8 * ks, bh, id2, 1u);
+            if (XLO) mma_bf16_tmem_a(tmem + COL_D2, rh + 8 * ks, desc_feats(xl, h, ks), id2, 1u);
+          }
+          mma_commit(&bars[B_REMPTY + b]);
+          if (h == 1) mma_commit(&bars[B_XEMPTY + st]);
+          return true;
+        };
+        for (int p = 0; p < passes && ok; ++p) {
+          const int i = p >> 1, h = p & 1, st = i % STAGES, b = p & 1;
+          if (h == 0)
+            ok = mbar_wait_abortable(&bars[B_XFULL + st], (i / STAGES) & 1, abort_s, a.err, 24);
+          ok = ok && mbar_wait_abortable(&bars[B_D1EMPTY + b], ((p >> 1) & 1) ^ 1, abort_s,
+                                         a.err, 25);
+          if (!ok) break;
+          fence_after_sync();
+          const uint32_t xh = smem_u32(sm + SMEM_X + st * STAGE_BYTES);
+          const uint32_t xl = xh + PART_BYTES;
+          const uint32_t d1 = tmem + COL_D1 + 64 * b;
+#pragma unroll 1
+          for (int ks = 0; ks < TK / 16; ++ks) {
+            const uint64_t bh = desc_rows(xh, h, ks);
+            mma_bf16_tmem_a(d1, tmem + COL_TH + 8 * ks, bh, id1, ks > 0 ? 1u : 0u);
+            mma_bf16_tmem_a(d1, tmem + COL_TL + 8 * ks, bh, id1, 1u);
+            if (XLO) mma_bf16_tmem_a(d1, tmem + COL_TH + 8 * ks, desc_rows(xl, h, ks), id1, 1u);
+          }
+          mma_commit(&bars[B_D1FULL + b]);
+          if (p > 0) ok = gemm2(p - 1);
+        }
+        if (ok) ok = gemm2(passes - 1);
+        mma_commit(&bars[B_D2FULL]);
+        // no MMA may still run when tensor memory is released
+        mbar_wait(&bars[B_D2FULL], 0, a.err, 29);
+      }
+      __syncwarp();
+    } else {
+      // ---- epilogue: warp w owns TMEM lane quarter q = w % 4 (chains
+      // 32q..32q+31) and half hw of each pass's rows / of the features.
+      const int q = warp & 3;
+      const int hw = (warp - 2) >> 2;
+      const int c = 32 * q + lane;
+      const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
+      // Theta (this chain, features 64hw..64hw+63) -> TMEM, bf16 hi / lo pairs
+      {
+        const bool act = act_s[c] != 0;
+        const double* th = a.Q + (size_t)(act ? c0 + c : 0) * a.ldq;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          uint32_t wh[16], wl[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int k = 64 * hw + 32 * half + 2 * j;
+            const double d0 = (act && k < Kx) ? th[k] : 0.0;
+            const double d1 = (act && k + 1 < Kx) ? th[k + 1] : 0.0;
+            const __nv_bfloat16 h0 = __double2bfloat16(d0), h1 = __double2bfloat16(d1);
+            const __nv_bfloat16 l0 = __float2bfloat16_rn((float)(d0 - (double)__bfloat162float(h0)));
+            const __nv_bfloat16 l1 = __float2bfloat16_rn((float)(d1 - (double)__bfloat162float(h1)));
+            wh[j] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+            wl[j] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+          }
+          tmem_st16(lane_addr + COL_TH + 32 * hw + 16 * half, wh);
+          tmem_st16(lane_addr + COL_TL + 32 * hw + 16 * half, wl);
+        }
+        tmem_st_wait();
+        fence_before_sync();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bars[B_THETA]);
+      }
+      double lp_acc = 0.0;
+      bool ok = true;
+      for (int p = 0; p < passes && ok; ++p) {
+        const int i = p >> 1, h = p & 1, st = i % STAGES, b = p & 1;
+        if (!warp_wait(&bars[B_D1FULL + b], (p >> 1) & 1, abort_s, a.err, 26)) {
+          ok = false;
+          break;
+        }
+        fence_after_sync();
+        float v[32];
+        tmem_ld32(lane_addr + COL_D1 + 64 * b + 32 * hw, v);
+        tmem_ld_wait();
+        fence_before_sync();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bars[B_D1EMPTY + b]);
+        const float* ys =
+            reinterpret_cast<const float*>(sm + SMEM_X + st * STAGE_BYTES + 2 * PART_BYTES);
+        const int rr0 = 64 * h + 32 * hw;
+        const long long row0 = (long long)(t_begin + i) * TM + rr0;
+        const int nvalid = (int)max(0LL, min(32LL, a.N - row0));
+        float lp_t = 0.f;
+        uint32_t wh[16], wl[16];
+#pragma unroll
+        for (int j = 0; j < 32; j += 2) {
+          float res[2];
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const float eta = v[j + e];
+            const float yv = ys[rr0 + j + e];
+            float term, resid;
+            if (LINK == LINK_LOGIT) {
+              const float ex = __expf(-fabsf(eta));
+              const float d = 1.f + ex;
+              const float inv = __fdividef(1.f, d);
+              const float sig = eta >= 0.f ? inv : ex * inv;
+              term = yv * eta - (fmaxf(eta, 0.f) + __logf(d));
+              resid = yv - sig;
+            } else {
+              const float mu = __expf(eta);
+              term = yv * eta - mu;
+              resid = yv - mu;
+            }
+            const bool valid = j + e < nvalid;
+            lp_t += valid ? term : 0.f;
+            res[e] = valid ? resid : 0.f;
+          }
+          const __nv_bfloat162 hp = __floats2bfloat162_rn(res[0], res[1]);
+          const float2 hf = __bfloat1622float2(hp);
+          const __nv_bfloat162 lp2 = __floats2bfloat162_rn(res[0] - hf.x, res[1] - hf.y);
+          wh[j >> 1] = *reinterpret_cast<const uint32_t*>(&hp);
+          wl[j >> 1] = *reinterpret_cast<const uint32_t*>(&lp2);
+        }
+        lp_acc += (double)lp_t;
+        if (!warp_wait(&bars[B_REMPTY + b], ((p >> 1) & 1) ^ 1, abort_s, a.err, 27)) {
+          ok = false;
+          break;
+        }
+        fence_after_sync();
+        tmem_st16(lane_addr + COL_R + 64 * b + 16 * hw, wh);
+        tmem_st16(lane_addr + COL_R + 64 * b + 32 + 16 * hw, wl);
+        tmem_st_wait();
+        fence_before_sync();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bars[B_RFULL + b]);
+      }
+      sLP[hw * NCH + c] = lp_acc;
+      // gradient partials: this chain's features 64hw..64hw+63
+      if (ok && warp_wait(&bars[B_D2FULL], 0, abort_s, a.err, 28)) {
+        fence_after_sync();
+        float g[64];
+        tmem_ld32(lane_addr + COL_D2 + 64 * hw, g);
+        tmem_ld32(lane_addr + COL_D2 + 64 * hw + 32, g + 32);
+        tmem_ld_wait();
+        if (act_s[c]) {
+          double* dst = a.P + ((size_t)s * a.C + c0 + c) * a.NP;
+#pragma unroll
+          for (int j = 0; j < 64; ++j) {
+            const int k = 64 * hw + j;
+            if (k < hb)
+              dst[1] = (double)g[j];
+            else if (k < Kx)
+              dst[4 + (k - hb)] = (double)g[j];
+          }
+        }
+      }
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (tid < NCH && act_s[tid]) {
+    double* dst = a.P + ((size_t)s * a.C + c0 + tid) * a.NP;
+    double lp = 0.0;
+    if (n > 0) lp = sLP[tid] + sLP[NCH + tid];
+    dst[0] = lp;
+    dst[2] = 0.0;
+    dst[3] = 0.0;
+    if (n == 0) {
+      for (int k = 0; k < Kx; ++k) dst[k < hb ? 1 : 4 + (k - hb)] = 0.0;
+    }
+  }
+  if (warp == 0) {
+    fence_after_sync();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+int tct_splits(const ModelDesc& m, int C) {
+  const int groups = (C + tct::NCH - 1) / tct::NCH;
+  int S = std::max(1, 148 / groups);
+  S = std::min<long long>(S, std::max(1, m.tc_tiles));
+  return S;
+}
+
+int launch_tct(const ModelDesc& m, const double* Q, int ldq, int C, const int* active,
+               GradWorkspace& ws, cudaStream_t st) {
+  using namespace tct;
+  static bool attr = false;
+  if (!attr) {
+    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tct_kernel<LINK_LOGIT, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
+    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tct_kernel<LINK_LOGIT, false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
+    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tct_kernel<LINK_POISSON_LOG, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
+    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tct_kernel<LINK_POISSON_LOG, false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
+    attr = true;
+  }
+  TctArgs a;
+  a.xt = static_cast<const __nv_bfloat16*>(m.tc_xt);
+  a.yt = m.tc_yt;
+  a.N = m.N;
+  a.K = m.K;
+  a.has_base = m.has_base;
+  a.n_tiles = m.tc_tiles;
+  a.Q = Q;
+  a.ldq = ldq;
+  a.C = C;
+  a.active = active;
+  a.P = ws.partial;
+  a.NP = ws.NP;
+  a.S = ws.S;
+  a.err = ws.err;
+  const bool xlo = m.x_dtype != GBNUTS_BF16;
+  dim3 grid(ws.S, (C + NCH - 1) / NCH);
+  if (m.link == LINK_LOGIT) {
+    if (xlo)
+      glm_tct_kernel<LINK_LOGIT, true><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
+    else
+      glm_tct_kernel<LINK_LOGIT, false><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
+  } else {
+    if (xlo)
+      glm_tct_kernel<LINK_POISSON_LOG, true><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
+    else
+      glm_tct_kernel<LINK_POISSON_LOG, false><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
+  }
+  GBN_CUDA_TRY(cudaGetLastError());
+  return GBNUTS_OK;
+}
+
+// ------------------------------------------------------------------ probe
+// Checks the tensor-memory A operand and both B layouts on one tile:
+// D1 = A . X^T (A: 128 x 128 in TMEM from Aw, X: 128 rows x 128 features),
+// D2 = R . X   (R: 128 x 128 rows in TMEM from Rw).  Aw, Rw: 128 lanes x 64
+// 32-bit words each, written to TMEM as given.
+__global__ void __launch_bounds__(128, 1)
+    tct_probe_kernel(const uint32_t* Aw, const __nv_bfloat16* X, const uint32_t* Rw, float* D1,
+                     float* D2, int* err) {
+  using namespace tct;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  unsigned char* sX = sm;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + PART_BYTES);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + PART_BYTES + 16);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < TM * TK; i += 128) {
+    const int r = i / TK, k = i - r * TK;
+    *reinterpret_cast<__nv_bfloat16*>(sX + kmajor_off(r, k, TK)) = X[i];
+  }
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, 512);
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+  for (int j = 0; j < 64; j += 16) {
+    uint32_t a[16], r[16];
+    for (int i = 0; i < 16; ++i) {
+      a[i] = Aw[tid * 64 + j + i];
+      r[i] = Rw[tid * 64 + j + i];
+    }
+    tmem_st16(lane_base + 256 + j, a);
+    tmem_st16(lane_base + 320 + j, r);
+  }
+  tmem_st_wait();
+  fence_proxy_async();
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  if (tid == 0) {
+    const uint32_t sx = smem_u32(sX);
+    const uint32_t id1 = make_idesc_bf16(128, 64, 0, 0);
+    const uint32_t id2 = make_idesc_bf16(128, 128, 0, 1);
+    for (int h = 0; h < 2; ++h)
+      for (int ks = 0; ks < TK / 16; ++ks)
+        mma_bf16_tmem_a(tmem + 64 * h, tmem + 256 + 8 * ks, desc_rows(sx, h, ks), id1, ks > 0);
+    for (int h = 0; h < 2; ++h)
+      for (int ks = 0; ks < HR / 16; ++ks)
+        mma_bf16_tmem_a(tmem + 128, tmem + 320 + 32 * h + 8 * ks, desc_feats(sx, h, ks), id2,
+                        (h | ks) != 0);
+    mma_commit(bar);
+  }
+  const bool ok = mbar_wait(bar, 0, err, 3);
+  fence_after_sync();
+  if (ok) {
+    float v[32];
+    for (int j = 0; j < 128; j += 32) {
+      tmem_ld32(lane_base + j, v);
+      tmem_ld_wait();
+      for (int c = 0; c < 32; ++c) D1[tid * 128 + j + c] = v[c];
+      tmem_ld32(lane_base + 128 + j, v);
+      tmem_ld_wait();
+      for (int c = 0; c < 32; ++c) D2[tid * 128 + j + c] = v[c];
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after_sync();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+}  // namespace gbn
+
+// Test hook (include/gbnuts_testing.h): runs the probe kernel on host arrays.
+extern "C" int gbnuts_tct_probe(const uint32_t* Aw, const uint16_t* X, const uint32_t* Rw,
+                                float* D1, float* D2) {
+  using namespace gbn;
+  using namespace gbn::tct;
+  void *dA, *dX, *dR, *dD1, *dD2, *dE;
+  GBN_CUDA_TRY(cudaMalloc(&dA, 128 * 64 * 4));
+  GBN_CUDA_TRY(cudaMalloc(&dX, TM * TK * 2));
+  GBN_CUDA_TRY(cudaMalloc(&dR, 128 * 64 * 4));
+  GBN_CUDA_TRY(cudaMalloc(&dD1, 128 * 128 * 4));
+  GBN_CUDA_TRY(cudaMalloc(&dD2, 128 * 128 * 4));
+  GBN_CUDA_TRY(cudaMalloc(&dE, 4));
+  GBN_CUDA_TRY(cudaMemset(dE, 0, 4));
+  GBN_CUDA_TRY(cudaMemcpy(dA, Aw, 128 * 64 * 4, cudaMemcpyHostToDevice));
+  GBN_CUDA_TRY(cudaMemcpy(dX, X, TM * TK * 2, cudaMemcpyHostToDevice));
+  GBN_CUDA_TRY(cudaMemcpy(dR, Rw, 128 * 64 * 4, cudaMemcpyHostToDevice));
+  const int smem = PART_BYTES + 64 + 1024;
+  GBN_CUDA_TRY(cudaFuncSetAttribute(tct_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    smem));
+  tct_probe_kernel<<<1, 128, smem>>>((const uint32_t*)dA, (const __nv_bfloat16*)dX,
+                                     (const uint32_t*)dR, (float*)dD1, (float*)dD2, (int*)dE);
+  GBN_CUDA_TRY(cudaGetLastError());
+  GBN_CUDA_TRY(cudaDeviceSynchronize());
+  int e = 0;
+  GBN_CUDA_TRY(cudaMemcpy(&e, dE, 4, cudaMemcpyDeviceToHost));
+  GBN_CUDA_TRY(cudaMemcpy(D1, dD1, 128 * 128 * 4, cudaMemcpyDeviceToHost));
+  GBN_CUDA_TRY(cudaMemcpy(D2, dD2, 128 * 128 * 4, cudaMemcpyDeviceToHost));
+  cudaFree(dA);
+  cudaFree(dX);
+  cudaFree(dR);
+  cudaFree(dD1);
+  cudaFree(dD2);
+  cudaFree(dE);
+  if (e) {
+    set_last_error("tensor-core probe: wait timed out");
+    return GBNUTS_SOFTWARE;
+  }
+  return GBNUTS_OK;
+}

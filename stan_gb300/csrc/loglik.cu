@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <mutex>
 #include <stdlib.h>
+#include <string.h>
 
 #include "../../include/gbnuts.h"
 #include "gbnuts_internal.h"
@@ -418,18 +419,26 @@ int launch_partials_pool(const PoolGradFit* d_fits, const PoolWorkItem* d_items,
              : launch_pool_t<uint16_t, float>(d_fits, d_items, n_items, smem, st);
 }
 
+bool tc_chains_on_m() {
+  static const bool v = [] {
+    const char* e = getenv("GBNUTS_TC_KERNEL");
+    return !(e && strcmp(e, "m64") == 0);
+  }();
+  return v;
+}
+
 // Minimum rows of a split (GBNUTS_SPLIT_ROWS overrides it, for tuning).
 static long long split_rows_min() {
   static const long long v = [] {
     const char* e = getenv("GBNUTS_SPLIT_ROWS");
     const long long r = e ? atoll(e) : 0;
-    return r > 0 ? r : 64LL;
+    return r > 0 ? r : 256LL;
   }();
   return v;
 }
 
 int choose_splits(const ModelDesc& m, int C, int precision) {
-  if (precision == GBNUTS_PREC_BF16X3) return tc_splits(m, C);
+  if (precision == GBNUTS_PREC_BF16X3) return tc_chains_on_m() ? tct_splits(m, C) : tc_splits(m, C);
   const int CB = chains_per_block(m.K);
   const int chain_blocks = (C + CB - 1) / CB;
   // Splits: enough CTAs for ~2 waves over 152 SMs, a minimum of rows each.
@@ -505,7 +514,8 @@ int launch_partials(const ModelDesc& m, int precision, const double* Q, int ldq,
   } else if (precision == GBNUTS_PREC_FP32) {
     dispatch_x<float>(m, Q, ldq, C, active, ws, stream);
   } else if (precision == GBNUTS_PREC_BF16X3 && m.tc_xt != nullptr) {
-    int rc = launch_tc(m, Q, ldq, C, active, ws, stream);
+    int rc = tc_chains_on_m() ? launch_tct(m, Q, ldq, C, active, ws, stream)
+                              : launch_tc(m, Q, ldq, C, active, ws, stream);
     if (rc) return rc;
   } else {
     set_last_error("precision not available for this model");

@@ -42,6 +42,39 @@ def test_descriptor_probe_exact():
     assert np.array_equal(D2, A.T @ R), "MN-major contraction (X^T . R) differs"
 
 
+def test_tensor_memory_operand_probe_exact():
+    """A operands in tensor memory: word j of lane m holds elements 2j (low
+    half) and 2j + 1 (high half) of row m."""
+    from stan_gb300 import _lib
+    lib = _lib.load()
+    f = lib.gbnuts_tct_probe
+    u16 = ctypes.POINTER(ctypes.c_uint16)
+    u32 = ctypes.POINTER(ctypes.c_uint32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    f.restype = ctypes.c_int
+    f.argtypes = [u32, u16, u32, fp, fp]
+    rng = np.random.default_rng(1)
+    A = rng.integers(-2, 3, size=(128, 128)).astype(np.float32)
+    X = rng.integers(-2, 3, size=(128, 128)).astype(np.float32)
+    R = rng.integers(-2, 3, size=(128, 128)).astype(np.float32)
+
+    def words(M):
+        b = _bf16_bits(M).astype(np.uint32)
+        return np.ascontiguousarray(b[:, 0::2] | (b[:, 1::2] << 16), dtype=np.uint32)
+
+    aw, rw, xb = words(A), words(R), _bf16_bits(X)
+    D1 = np.zeros((128, 128), dtype=np.float32)
+    D2 = np.zeros((128, 128), dtype=np.float32)
+    rc = f(aw.ctypes.data_as(u32), xb.ctypes.data_as(u16), rw.ctypes.data_as(u32),
+           D1.ctypes.data_as(fp), D2.ctypes.data_as(fp))
+    assert rc == 0, _lib.last_error()
+    swapped = A.reshape(128, 64, 2)[:, :, ::-1].reshape(128, 128)
+    assert np.array_equal(D1, A @ X.T), (
+        "A-in-TMEM contraction differs" +
+        (" (halves swapped)" if np.array_equal(D1, swapped @ X.T) else ""))
+    assert np.array_equal(D2, R @ X), "MN-major B contraction differs"
+
+
 @pytest.mark.parametrize("kind", ["logistic", "logistic_100k", "poisson"])
 def test_bf16x3_gradient_matches_fp64_oracle(kind):
     from stan_gb300 import Model
