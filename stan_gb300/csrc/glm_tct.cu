@@ -2,22 +2,25 @@
 // the M dimension (precision GBNUTS_PREC_BF16X3, logistic and Poisson).
 //
 // A CTA owns 128 chains (one per TMEM lane) and a range of 128-row tiles of X,
-// taken 64 rows at a time:
-//   GEMM1  eta^T (128 chains x 64 rows)  = Theta . X_half^T      A = Theta in TMEM
-//   link   term, r = d lp / d eta        per (chain, row), fp32, read from TMEM
-//   GEMM2  G^T (128 chains x 128 feats) += R . X_half             A = R in TMEM
+// one tile per pass:
+//   GEMM1  eta^T (128 chains x 128 rows)  = Theta . X_tile^T     A = Theta in TMEM
+//   link   term, r = d lp / d eta         per (chain, row), fp32, read from TMEM
+//   GEMM2  G^T (128 chains x NF feats)   += R . X_tile           A = R in TMEM
 // Theta and R are A operands held in tensor memory (bf16 hi and lo parts,
 // two elements per 32-bit column), so every MMA reads only its X operand
 // from shared memory: GEMM1 reads X K-major (rows x features) and GEMM2 the
-// same bytes MN-major (features x rows).  X, Theta and R are each split into
-// bf16 hi + lo and the three products hi.hi + hi.lo + lo.hi accumulate in
-// fp32 (x has no lo part when stored in bf16).  Each epilogue thread owns one
-// chain, so the lp sum over rows stays in the thread.
+// same bytes MN-major (features x rows).  An MMA instruction costs about the
+// same time for any N up to 128, so GEMM1 takes a whole 128-row tile as N,
+// and contraction steps past the last feature are skipped.  X, Theta and R
+// are each split into bf16 hi + lo and the three products hi.hi + hi.lo +
+// lo.hi accumulate in fp32 (x has no lo part when stored in bf16).  Theta is
+// scaled by log2(e), so eta comes out in base-2 units for the MUFU ex2 / lg2.
+// Each epilogue thread owns one chain, so the lp sum over rows stays in the
+// thread (a compensated fp32 sum).
 //
-// TMEM columns (512): eta^T double buffer [0, 128), G^T [128, 256), Theta hi
-// [256, 320) and lo [320, 384), R double buffer [384, 512) (hi 32 + lo 32
-// columns per 64 rows).  Shared memory: a 3-stage ring of 128-row X tiles
-// (hi + lo + y, 65 KiB each).
+// TMEM columns (512): eta^T [0, 128), G^T [128, 256), Theta hi [256, 320) and
+// lo [320, 384), R hi [384, 448) and lo [448, 512).  Shared memory: a 3-stage
+// ring of 128-row X tiles (hi + lo + y, 65 KiB each).
 #include <cuda_bf16.h>
 #include <math.h>
 
@@ -34,32 +37,36 @@ using namespace tc;
 namespace tct {
 
 constexpr int TM = 128;            // rows per pre-tiled X tile
-constexpr int HR = 64;             // rows per GEMM1 / epilogue / GEMM2 pass
 constexpr int TK = 128;            // features per tile (K + intercept, zero padded)
 constexpr int NCH = 128;           // chains per CTA (TMEM lanes)
 constexpr int PART_BYTES = TM * TK * 2;   // one bf16 part of an X tile
-constexpr int HALF_BYTES = HR * TK * 2;   // rows [64h, 64h+64) of a part
 constexpr int Y_BYTES = TM * 4;
 constexpr int STAGE_BYTES = 2 * PART_BYTES + 1024;  // X hi, X lo, y (padded)
 constexpr int STAGES = 3;
-constexpr int NUM_EPI_WARPS = 8;   // two per TMEM lane quarter
+constexpr int NUM_EPI_WARPS = 16;  // four per TMEM lane quarter
+constexpr int EPI_SUB = NUM_EPI_WARPS / 4;
+constexpr int RW = TM / EPI_SUB;   // rows of a pass per epilogue warp
+constexpr int FW = TK / EPI_SUB;   // features per epilogue warp (gradient readout)
 constexpr int THREADS = 64 + 32 * NUM_EPI_WARPS;
 constexpr int SMEM_X = 0;
-constexpr int SMEM_LP = SMEM_X + STAGES * STAGE_BYTES;   // [2][NCH] doubles
-constexpr int SMEM_BAR = SMEM_LP + 2 * NCH * 8;
+constexpr int SMEM_LP = SMEM_X + STAGES * STAGE_BYTES;   // [EPI_SUB][NCH] doubles
+constexpr int SMEM_BAR = SMEM_LP + EPI_SUB * NCH * 8;
+constexpr double kLn2 = 0.69314718055994530942;
+constexpr float kLog2ef = 1.44269504f;
 constexpr int SMEM_TOTAL = SMEM_BAR + 256;
 constexpr int SMEM_ALLOC = SMEM_TOTAL + 1024;  // slack for 1 KiB alignment
 // TMEM column map
-constexpr uint32_t COL_D1 = 0, COL_D2 = 128, COL_TH = 256, COL_TL = 320, COL_R = 384;
+constexpr uint32_t COL_D1 = 0, COL_D2 = 128, COL_TH = 256, COL_TL = 320, COL_RH = 384,
+                   COL_RL = 448;
 
-// GEMM1 B operand: rows [64h, 64h+64) of a K-major tile part, features ks*16.
-__device__ __forceinline__ uint64_t desc_rows(uint32_t part, int h, int ks) {
-  return make_desc(part + h * HALF_BYTES + 256 * ks, 128, (TK / 8) * 128);
+// GEMM1 B operand: the 128 rows of a K-major tile part, features 16ks..16ks+15.
+__device__ __forceinline__ uint64_t desc_rows(uint32_t part, int ks) {
+  return make_desc(part + 256 * ks, 128, (TK / 8) * 128);
 }
 // GEMM2 B operand: the same part read MN-major (features x rows), rows
-// 64h + 16ks .. +16.
-__device__ __forceinline__ uint64_t desc_feats(uint32_t part, int h, int ks) {
-  return make_desc(part + h * HALF_BYTES + 4096 * ks, (TK / 8) * 128, 128);
+// 16ks..16ks+15.
+__device__ __forceinline__ uint64_t desc_feats(uint32_t part, int ks) {
+  return make_desc(part + 4096 * ks, (TK / 8) * 128, 128);
 }
 
 }  // namespace tct
@@ -79,9 +86,69 @@ struct TctArgs {
 
 namespace tct {
 // barrier slots (uint64 each) inside SMEM_BAR
-enum { B_XFULL = 0, B_XEMPTY = 3, B_D1FULL = 6, B_D1EMPTY = 8, B_RFULL = 10, B_REMPTY = 12,
-       B_D2FULL = 14, B_THETA = 15, B_COUNT = 16 };
+enum { B_XFULL = 0, B_XEMPTY = 3, B_D1FULL = 6, B_D1EMPTY = 7, B_RFULL = 8, B_REMPTY = 9,
+       B_D2FULL = 10, B_THETA = 11, B_COUNT = 12 };
 }  // namespace tct
+
+// Link terms of one pass for one chain: e2[j] = log2(e) eta of rows
+// rr0 + j, y[j] their outcomes.  Accumulates pa, pb with lp = ln2 pa - pb
+// (logistic: pa = sum y e2 - max(e2, 0) - log2(1 + 2^-|e2|), pb = 0;
+// Poisson: pa = sum y e2, pb = sum mu) and packs r = y - mean as bf16 hi / lo
+// pairs.  MASK: rows j >= nvalid (past N) contribute nothing.
+template <int LINK, bool MASK, int RWN>
+__device__ __forceinline__ void epilogue_values(const float* e2, const float* y, int nvalid,
+                                                float& pa, float& pb, uint32_t* wh,
+                                                uint32_t* wl) {
+#pragma unroll
+  for (int j = 0; j < RWN; j += 4) {
+    const float4 y4 = *reinterpret_cast<const float4*>(y + j);
+    const float yv[4] = {y4.x, y4.y, y4.z, y4.w};
+    float res[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float x = e2[j + e];
+      float ta, tb = 0.f, r;
+      if (LINK == LINK_LOGIT) {
+        const float ex = ex2_approx(-fabsf(x));
+        const float d = 1.f + ex;
+        const float inv = rcp_approx(d);
+        const float sig = x >= 0.f ? inv : ex * inv;
+        ta = yv[e] * x - fmaxf(x, 0.f) - lg2_approx(d);
+        r = yv[e] - sig;
+      } else {
+        const float mu = ex2_approx(x);
+        ta = yv[e] * x;
+        tb = mu;
+        r = yv[e] - mu;
+      }
+      if (MASK && j + e >= nvalid) {
+        ta = 0.f;
+        tb = 0.f;
+        r = 0.f;
+      }
+      pa += ta;
+      if (LINK != LINK_LOGIT) pb += tb;
+      res[e] = r;
+    }
+#pragma unroll
+    for (int e = 0; e < 4; e += 2) {
+      const __nv_bfloat162 hp = __floats2bfloat162_rn(res[e], res[e + 1]);
+      const float2 hf = __bfloat1622float2(hp);
+      const __nv_bfloat162 lo = __floats2bfloat162_rn(res[e] - hf.x, res[e + 1] - hf.y);
+      wh[(j + e) >> 1] = *reinterpret_cast<const uint32_t*>(&hp);
+      wl[(j + e) >> 1] = *reinterpret_cast<const uint32_t*>(&lo);
+    }
+  }
+}
+
+// s += v as an unevaluated fp32 pair (s.x + s.y), Knuth's two-sum.
+__device__ __forceinline__ void two_sum_add(float2& s, float v) {
+  const float t = s.x + v;
+  const float bp = t - s.x;
+  const float err = (s.x - (t - bp)) + (v - bp);
+  s.x = t;
+  s.y += err;
+}
 
 template <int LINK, bool XLO>
 __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
@@ -113,12 +180,10 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
       mbar_init(&bars[B_XFULL + b], 1);
       mbar_init(&bars[B_XEMPTY + b], 1);
     }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&bars[B_D1FULL + b], 1);
-      mbar_init(&bars[B_D1EMPTY + b], NUM_EPI_WARPS);
-      mbar_init(&bars[B_RFULL + b], NUM_EPI_WARPS);
-      mbar_init(&bars[B_REMPTY + b], 1);
-    }
+    mbar_init(&bars[B_D1FULL], 1);
+    mbar_init(&bars[B_D1EMPTY], NUM_EPI_WARPS);
+    mbar_init(&bars[B_RFULL], NUM_EPI_WARPS);
+    mbar_init(&bars[B_REMPTY], 1);
     mbar_init(&bars[B_D2FULL], 1);
     mbar_init(&bars[B_THETA], NUM_EPI_WARPS);
     *abort_s = 0;
@@ -133,8 +198,9 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
   const int t_begin = (int)((long long)a.n_tiles * s / a.S);
   const int t_end = (int)((long long)a.n_tiles * (s + 1) / a.S);
   const int n = t_end - t_begin;
-  const int passes = 2 * n;
   const uint32_t x_bytes = XLO ? 2u * PART_BYTES : (uint32_t)PART_BYTES;
+  const int ksteps = (Kx + 15) / 16;   // GEMM1 contraction steps holding features
+  const int nf = 16 * ksteps;          // GEMM2 N: features rounded up to 16
 
   if (n > 0) {
     if (warp == 0) {
@@ -155,54 +221,49 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
       }
       __syncwarp();
     } else if (warp == 1) {
-      // ---- MMA issuer: GEMM1 of pass p, then GEMM2 of pass p - 1
+      // ---- MMA issuer: GEMM1 of tile i, then GEMM2 of tile i - 1
       if (lane == 0) {
-        const uint32_t id1 = make_idesc_bf16(NCH, HR, 0, 0);
-        const uint32_t id2 = make_idesc_bf16(NCH, TK, 0, 1);
+        const uint32_t id1 = make_idesc_bf16(NCH, TM, 0, 0);
+        const uint32_t id2 = make_idesc_bf16(NCH, nf, 0, 1);
         bool ok = mbar_wait_abortable(&bars[B_THETA], 0, abort_s, a.err, 22);
         fence_after_sync();
-        auto gemm2 = [&](int p) -> bool {
-          const int b = p & 1;
-          if (!mbar_wait_abortable(&bars[B_RFULL + b], (p >> 1) & 1, abort_s, a.err, 23))
-            return false;
+        auto gemm2 = [&](int i) -> bool {
+          if (!mbar_wait_abortable(&bars[B_RFULL], i & 1, abort_s, a.err, 23)) return false;
           fence_after_sync();
-          const int i = p >> 1, h = p & 1, st = i % STAGES;
+          const int st = i % STAGES;
           const uint32_t xh = smem_u32(sm + SMEM_X + st * STAGE_BYTES);
           const uint32_t xl = xh + PART_BYTES;
-          const uint32_t rh = tmem + COL_R + 64 * b, rl = rh + 32;
 #pragma unroll 1
-          for (int ks = 0; ks < HR / 16; ++ks) {
-            const uint64_t bh = desc_feats(xh, h, ks);
-            mma_bf16_tmem_a(tmem + COL_D2, rh + 8 * ks, bh, id2, (p > 0 || ks > 0) ? 1u : 0u);
-            mma_bf16_tmem_a(tmem + COL_D2, rl + 8 * ks, bh, id2, 1u);
-            if (XLO) mma_bf16_tmem_a(tmem + COL_D2, rh + 8 * ks, desc_feats(xl, h, ks), id2, 1u);
+          for (int ks = 0; ks < TM / 16; ++ks) {
+            const uint64_t bh = desc_feats(xh, ks);
+            mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RH + 8 * ks, bh, id2,
+                            (i > 0 || ks > 0) ? 1u : 0u);
+            mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RL + 8 * ks, bh, id2, 1u);
+            if (XLO) mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RH + 8 * ks, desc_feats(xl, ks), id2, 1u);
           }
-          mma_commit(&bars[B_REMPTY + b]);
-          if (h == 1) mma_commit(&bars[B_XEMPTY + st]);
+          mma_commit(&bars[B_REMPTY]);
+          mma_commit(&bars[B_XEMPTY + st]);
           return true;
         };
-        for (int p = 0; p < passes && ok; ++p) {
-          const int i = p >> 1, h = p & 1, st = i % STAGES, b = p & 1;
-          if (h == 0)
-            ok = mbar_wait_abortable(&bars[B_XFULL + st], (i / STAGES) & 1, abort_s, a.err, 24);
-          ok = ok && mbar_wait_abortable(&bars[B_D1EMPTY + b], ((p >> 1) & 1) ^ 1, abort_s,
-                                         a.err, 25);
+        for (int i = 0; i < n && ok; ++i) {
+          const int st = i % STAGES;
+          ok = mbar_wait_abortable(&bars[B_XFULL + st], (i / STAGES) & 1, abort_s, a.err, 24) &&
+               mbar_wait_abortable(&bars[B_D1EMPTY], (i & 1) ^ 1, abort_s, a.err, 25);
           if (!ok) break;
           fence_after_sync();
           const uint32_t xh = smem_u32(sm + SMEM_X + st * STAGE_BYTES);
           const uint32_t xl = xh + PART_BYTES;
-          const uint32_t d1 = tmem + COL_D1 + 64 * b;
 #pragma unroll 1
-          for (int ks = 0; ks < TK / 16; ++ks) {
-            const uint64_t bh = desc_rows(xh, h, ks);
-            mma_bf16_tmem_a(d1, tmem + COL_TH + 8 * ks, bh, id1, ks > 0 ? 1u : 0u);
-            mma_bf16_tmem_a(d1, tmem + COL_TL + 8 * ks, bh, id1, 1u);
-            if (XLO) mma_bf16_tmem_a(d1, tmem + COL_TH + 8 * ks, desc_rows(xl, h, ks), id1, 1u);
+          for (int ks = 0; ks < ksteps; ++ks) {
+            const uint64_t bh = desc_rows(xh, ks);
+            mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TH + 8 * ks, bh, id1, ks > 0 ? 1u : 0u);
+            mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TL + 8 * ks, bh, id1, 1u);
+            if (XLO) mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TH + 8 * ks, desc_rows(xl, ks), id1, 1u);
           }
-          mma_commit(&bars[B_D1FULL + b]);
-          if (p > 0) ok = gemm2(p - 1);
+          mma_commit(&bars[B_D1FULL]);
+          if (i > 0) ok = gemm2(i - 1);
         }
-        if (ok) ok = gemm2(passes - 1);
+        if (ok) ok = gemm2(n - 1);
         mma_commit(&bars[B_D2FULL]);
         // no MMA may still run when tensor memory is released
         mbar_wait(&bars[B_D2FULL], 0, a.err, 29);
@@ -210,115 +271,91 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
       __syncwarp();
     } else {
       // ---- epilogue: warp w owns TMEM lane quarter q = w % 4 (chains
-      // 32q..32q+31) and half hw of each pass's rows / of the features.
+      // 32q..32q+31), rows RW*sub.. of every tile and features FW*sub..
       const int q = warp & 3;
-      const int hw = (warp - 2) >> 2;
+      const int sub = (warp - 2) >> 2;
       const int c = 32 * q + lane;
       const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
-      // Theta (this chain, features 64hw..64hw+63) -> TMEM, bf16 hi / lo pairs
+      // log2(e) Theta of this chain -> TMEM as bf16 hi / lo pairs (fp32 split)
       {
         const bool act = act_s[c] != 0;
         const double* th = a.Q + (size_t)(act ? c0 + c : 0) * a.ldq;
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
+        for (int part = 0; part < FW / 32; ++part) {
           uint32_t wh[16], wl[16];
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            const int k = 64 * hw + 32 * half + 2 * j;
-            const double d0 = (act && k < Kx) ? th[k] : 0.0;
-            const double d1 = (act && k + 1 < Kx) ? th[k + 1] : 0.0;
-            const __nv_bfloat16 h0 = __double2bfloat16(d0), h1 = __double2bfloat16(d1);
-            const __nv_bfloat16 l0 = __float2bfloat16_rn((float)(d0 - (double)__bfloat162float(h0)));
-            const __nv_bfloat16 l1 = __float2bfloat16_rn((float)(d1 - (double)__bfloat162float(h1)));
-            wh[j] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-            wl[j] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+            const int k = FW * sub + 32 * part + 2 * j;
+            const float f0 = (act && k < Kx) ? (float)th[k] * kLog2ef : 0.f;
+            const float f1 = (act && k + 1 < Kx) ? (float)th[k + 1] * kLog2ef : 0.f;
+            const __nv_bfloat162 hp = __floats2bfloat162_rn(f0, f1);
+            const float2 hf = __bfloat1622float2(hp);
+            const __nv_bfloat162 lo = __floats2bfloat162_rn(f0 - hf.x, f1 - hf.y);
+            wh[j] = *reinterpret_cast<const uint32_t*>(&hp);
+            wl[j] = *reinterpret_cast<const uint32_t*>(&lo);
           }
-          tmem_st16(lane_addr + COL_TH + 32 * hw + 16 * half, wh);
-          tmem_st16(lane_addr + COL_TL + 32 * hw + 16 * half, wl);
+          tmem_st16(lane_addr + COL_TH + FW / 2 * sub + 16 * part, wh);
+          tmem_st16(lane_addr + COL_TL + FW / 2 * sub + 16 * part, wl);
         }
         tmem_st_wait();
         fence_before_sync();
         __syncwarp();
         if (lane == 0) mbar_arrive(&bars[B_THETA]);
       }
-      double lp_acc = 0.0;
+      float2 sa = make_float2(0.f, 0.f), sb = make_float2(0.f, 0.f);  // compensated
       bool ok = true;
-      for (int p = 0; p < passes && ok; ++p) {
-        const int i = p >> 1, h = p & 1, st = i % STAGES, b = p & 1;
-        if (!warp_wait(&bars[B_D1FULL + b], (p >> 1) & 1, abort_s, a.err, 26)) {
+      for (int i = 0; i < n && ok; ++i) {
+        const int st = i % STAGES;
+        if (!warp_wait(&bars[B_D1FULL], i & 1, abort_s, a.err, 26)) {
           ok = false;
           break;
         }
         fence_after_sync();
-        float v[32];
-        tmem_ld32(lane_addr + COL_D1 + 64 * b + 32 * hw, v);
+        float v[RW];
+        tmem_ld32(lane_addr + COL_D1 + RW * sub, v);
         tmem_ld_wait();
         fence_before_sync();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&bars[B_D1EMPTY + b]);
+        if (lane == 0) mbar_arrive(&bars[B_D1EMPTY]);
+        const int rr0 = RW * sub;
         const float* ys =
-            reinterpret_cast<const float*>(sm + SMEM_X + st * STAGE_BYTES + 2 * PART_BYTES);
-        const int rr0 = 64 * h + 32 * hw;
+            reinterpret_cast<const float*>(sm + SMEM_X + st * STAGE_BYTES + 2 * PART_BYTES) + rr0;
         const long long row0 = (long long)(t_begin + i) * TM + rr0;
-        const int nvalid = (int)max(0LL, min(32LL, a.N - row0));
-        float lp_t = 0.f;
-        uint32_t wh[16], wl[16];
-#pragma unroll
-        for (int j = 0; j < 32; j += 2) {
-          float res[2];
-#pragma unroll
-          for (int e = 0; e < 2; ++e) {
-            const float eta = v[j + e];
-            const float yv = ys[rr0 + j + e];
-            float term, resid;
-            if (LINK == LINK_LOGIT) {
-              const float ex = __expf(-fabsf(eta));
-              const float d = 1.f + ex;
-              const float inv = __fdividef(1.f, d);
-              const float sig = eta >= 0.f ? inv : ex * inv;
-              term = yv * eta - (fmaxf(eta, 0.f) + __logf(d));
-              resid = yv - sig;
-            } else {
-              const float mu = __expf(eta);
-              term = yv * eta - mu;
-              resid = yv - mu;
-            }
-            const bool valid = j + e < nvalid;
-            lp_t += valid ? term : 0.f;
-            res[e] = valid ? resid : 0.f;
-          }
-          const __nv_bfloat162 hp = __floats2bfloat162_rn(res[0], res[1]);
-          const float2 hf = __bfloat1622float2(hp);
-          const __nv_bfloat162 lp2 = __floats2bfloat162_rn(res[0] - hf.x, res[1] - hf.y);
-          wh[j >> 1] = *reinterpret_cast<const uint32_t*>(&hp);
-          wl[j >> 1] = *reinterpret_cast<const uint32_t*>(&lp2);
-        }
-        lp_acc += (double)lp_t;
-        if (!warp_wait(&bars[B_REMPTY + b], ((p >> 1) & 1) ^ 1, abort_s, a.err, 27)) {
+        const int nvalid = (int)max(0LL, min((long long)RW, a.N - row0));
+        float pa = 0.f, pb = 0.f;
+        uint32_t wh[RW / 2], wl[RW / 2];
+        if (nvalid == RW)
+          epilogue_values<LINK, false, RW>(v, ys, RW, pa, pb, wh, wl);
+        else
+          epilogue_values<LINK, true, RW>(v, ys, nvalid, pa, pb, wh, wl);
+        two_sum_add(sa, pa);
+        if (LINK != LINK_LOGIT) two_sum_add(sb, pb);
+        if (!warp_wait(&bars[B_REMPTY], (i & 1) ^ 1, abort_s, a.err, 27)) {
           ok = false;
           break;
         }
         fence_after_sync();
-        tmem_st16(lane_addr + COL_R + 64 * b + 16 * hw, wh);
-        tmem_st16(lane_addr + COL_R + 64 * b + 32 + 16 * hw, wl);
+        tmem_st16(lane_addr + COL_RH + RW / 2 * sub, wh);
+        tmem_st16(lane_addr + COL_RL + RW / 2 * sub, wl);
         tmem_st_wait();
         fence_before_sync();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&bars[B_RFULL + b]);
+        if (lane == 0) mbar_arrive(&bars[B_RFULL]);
       }
-      sLP[hw * NCH + c] = lp_acc;
-      // gradient partials: this chain's features 64hw..64hw+63
+      sLP[sub * NCH + c] =
+          kLn2 * ((double)sa.x + (double)sa.y) - ((double)sb.x + (double)sb.y);
+      // gradient partials: this chain's features FW*sub .. FW*sub + FW - 1
       if (ok && warp_wait(&bars[B_D2FULL], 0, abort_s, a.err, 28)) {
         fence_after_sync();
-        float g[64];
-        tmem_ld32(lane_addr + COL_D2 + 64 * hw, g);
-        tmem_ld32(lane_addr + COL_D2 + 64 * hw + 32, g + 32);
+        float g[FW];
+#pragma unroll
+        for (int j = 0; j < FW; j += 32) tmem_ld32(lane_addr + COL_D2 + FW * sub + j, g + j);
         tmem_ld_wait();
         if (act_s[c]) {
           double* dst = a.P + ((size_t)s * a.C + c0 + c) * a.NP;
 #pragma unroll
-          for (int j = 0; j < 64; ++j) {
-            const int k = 64 * hw + j;
+          for (int j = 0; j < FW; ++j) {
+            const int k = FW * sub + j;
             if (k < hb)
               dst[1] = (double)g[j];
             else if (k < Kx)
@@ -333,7 +370,8 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
   if (tid < NCH && act_s[tid]) {
     double* dst = a.P + ((size_t)s * a.C + c0 + tid) * a.NP;
     double lp = 0.0;
-    if (n > 0) lp = sLP[tid] + sLP[NCH + tid];
+    if (n > 0)
+      for (int k = 0; k < EPI_SUB; ++k) lp += sLP[k * NCH + tid];
     dst[0] = lp;
     dst[2] = 0.0;
     dst[3] = 0.0;
@@ -447,15 +485,12 @@ __global__ void __launch_bounds__(128, 1)
   fence_after_sync();
   if (tid == 0) {
     const uint32_t sx = smem_u32(sX);
-    const uint32_t id1 = make_idesc_bf16(128, 64, 0, 0);
+    const uint32_t id1 = make_idesc_bf16(128, 128, 0, 0);
     const uint32_t id2 = make_idesc_bf16(128, 128, 0, 1);
-    for (int h = 0; h < 2; ++h)
-      for (int ks = 0; ks < TK / 16; ++ks)
-        mma_bf16_tmem_a(tmem + 64 * h, tmem + 256 + 8 * ks, desc_rows(sx, h, ks), id1, ks > 0);
-    for (int h = 0; h < 2; ++h)
-      for (int ks = 0; ks < HR / 16; ++ks)
-        mma_bf16_tmem_a(tmem + 128, tmem + 320 + 32 * h + 8 * ks, desc_feats(sx, h, ks), id2,
-                        (h | ks) != 0);
+    for (int ks = 0; ks < TK / 16; ++ks)
+      mma_bf16_tmem_a(tmem + 0, tmem + 256 + 8 * ks, desc_rows(sx, ks), id1, ks > 0);
+    for (int ks = 0; ks < TM / 16; ++ks)
+      mma_bf16_tmem_a(tmem + 128, tmem + 320 + 8 * ks, desc_feats(sx, ks), id2, ks > 0);
     mma_commit(bar);
   }
   const bool ok = mbar_wait(bar, 0, err, 3);
