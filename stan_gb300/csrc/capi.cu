@@ -228,6 +228,10 @@ int gbnuts_model_create(int kind, const void* X, int x_dtype, const double* y,
       break;
   }
   d.sum_lgamma_y = sum_lgamma;
+  d.r_base2 = 1.0 / (d.s_base * d.s_base);
+  d.r_tau2 = 1.0 / (d.s_tau * d.s_tau);
+  d.r_sigma2 = 1.0 / (d.s_sigma * d.s_sigma);
+  d.r_beta2 = 1.0 / (d.s_beta * d.s_beta);
   const size_t xbytes = NK * (x_dtype == GBNUTS_F64 ? 8 : x_dtype == GBNUTS_F32 ? 4 : 2);
   cudaError_t e = cudaSuccess;
   if (xbytes) e = cudaMalloc(&m->d_X, xbytes);

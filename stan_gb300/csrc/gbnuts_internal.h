@@ -43,6 +43,7 @@ struct ModelDesc {
   const double* y;
   const int* group;  // N (hierarchical) or nullptr
   double s_base, s_tau, s_sigma, s_beta;  // prior scales
+  double r_base2, r_tau2, r_sigma2, r_beta2;  // 1 / scale^2 (set with the scales)
   double sum_lgamma_y;                    // Poisson constant, for propto = false
   // tensor-core form: X pre-tiled as bf16 hi/lo (128-row tiles), y per tile row
   const void* tc_xt;

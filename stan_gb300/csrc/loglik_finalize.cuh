@@ -2,8 +2,7 @@
 // partial sums: split sums in a fixed order (deterministic), priors, the
 // Jacobian of tau = exp(u), sigma = exp(u), and the chain rule through them.
 // One warp per chain, lanes over the coordinates; returns lp in every lane.
-// With many splits the split sums run with lanes over splits (a butterfly per
-// column) into a shared buffer, else with lanes over columns in split order.
+// The split sums go through a shared buffer first (split_column_sums).
 // Shared by the batched-gradient finalize kernel and the sampler step kernel.
 #pragma once
 
@@ -20,18 +19,37 @@ static constexpr int kMaxColSums = 4 + 512;
 // Splits from which the sums run with lanes over splits instead of columns.
 static constexpr int kLanesOverSplits = 32;
 
-// Column sums over the S splits of one chain's partials (row stride pstride),
-// lanes over splits, a fixed butterfly per column: cs[k] for k < NP.  The
-// order of additions depends on S and NP only.
+// Column sums over the S splits of one chain's partials (row stride pstride)
+// into cs[k], k < NP.  With many splits: lanes over splits and a fixed
+// butterfly per column.  Otherwise lanes over columns, adding the splits in
+// split order, their loads issued eight at a time.  The order of additions
+// depends on S and NP only.
 __device__ __forceinline__ void split_column_sums(const double* __restrict__ Pc, size_t pstride,
                                                   int S, int NP, double* cs, int lane) {
+  if (S >= kLanesOverSplits) {
 #pragma unroll 4
-  for (int k = 0; k < NP; ++k) {
-    double a = 0;
-    for (int s = lane; s < S; s += 32) a += Pc[s * pstride + k];
+    for (int k = 0; k < NP; ++k) {
+      double a = 0;
+      for (int s = lane; s < S; s += 32) a += Pc[s * pstride + k];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
-    if (lane == 0) cs[k] = a;
+      for (int off = 16; off > 0; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+      if (lane == 0) cs[k] = a;
+    }
+  } else {
+    for (int kb = 0; kb < NP; kb += 32) {
+      const int k = kb + lane;
+      double a = 0;
+      for (int s0 = 0; s0 < S; s0 += 8) {
+        double t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          t[u] = (k < NP && s0 + u < S) ? Pc[(size_t)(s0 + u) * pstride + k] : 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (s0 + u < S) a += t[u];
+      }
+      if (k < NP) cs[k] = a;
+    }
   }
   __syncwarp();
 }
@@ -45,7 +63,7 @@ __device__ __forceinline__ double finalize_chain(const ModelDesc& m, const doubl
                                                  int jacobian, int lane, double* cs) {
   const size_t pstride = (size_t)C * NP;
   const double* Pc = P + (size_t)c * NP;
-  const bool use_cs = S >= kLanesOverSplits && NP <= kMaxColSums;
+  const bool use_cs = NP <= kMaxColSums;
   if (use_cs) split_column_sums(Pc, pstride, S, NP, cs, lane);
   // sum over splits of partial column k (split order when lanes run over columns)
   auto col = [&](int k) -> double {
@@ -64,30 +82,26 @@ __device__ __forceinline__ double finalize_chain(const ModelDesc& m, const doubl
     if (d >= m.off_beta) {
       const int k = d - m.off_beta;
       const double sum = col(4 + k);
-      g = sum - t / (m.s_beta * m.s_beta);
-      const double z = t / m.s_beta;
-      prior += -0.5 * z * z;
+      g = sum - t * m.r_beta2;
+      prior += -0.5 * (t * t) * m.r_beta2;
       if (!propto) prior += -log(m.s_beta) - kLogSqrt2Pi;
     } else if (d == 0 && m.has_base) {
       const double sum = col(1);
-      g = sum - t / (m.s_base * m.s_base);
-      const double z = t / m.s_base;
-      prior += -0.5 * z * z;
+      g = sum - t * m.r_base2;
+      prior += -0.5 * (t * t) * m.r_base2;
       if (!propto) prior += -log(m.s_base) - kLogSqrt2Pi;
     } else if (d == m.idx_tau) {
       const double sum = col(2);
-      g = tau * (sum - tau / (m.s_tau * m.s_tau)) + jac;
-      const double z = tau / m.s_tau;
-      prior += -0.5 * z * z + jac * t;
+      g = tau * (sum - tau * m.r_tau2) + jac;
+      prior += -0.5 * (tau * tau) * m.r_tau2 + jac * t;
       if (!propto) prior += -log(m.s_tau) - kLogSqrt2Pi;
     } else if (d == m.idx_sigma) {
       const double sigma = exp(t);
       const double sum = col(3);
       const double dsig = -(double)m.N / sigma + sum / (sigma * sigma * sigma) -
-                          sigma / (m.s_sigma * m.s_sigma);
+                          sigma * m.r_sigma2;
       g = sigma * dsig + jac;
-      const double z = sigma / m.s_sigma;
-      prior += -0.5 * z * z + jac * t - (double)m.N * t;
+      prior += -0.5 * (sigma * sigma) * m.r_sigma2 + jac * t - (double)m.N * t;
       if (!propto) prior += -log(m.s_sigma) - kLogSqrt2Pi;
     } else {  // z_j
       const int j = d - m.off_z;

@@ -84,6 +84,7 @@ struct Stk {
 static __device__ double kinetic(const Ctx& x, const double* p) {
   const double* im = x.slot(SL_INVM);
   double s = 0.0;
+#pragma unroll 4
   for (int i = x.lane; i < x.cfg.D; i += 32) s += p[i] * DMUL(im[i], p[i]);
   return 0.5 * warp_sum(s);
 }
@@ -102,19 +103,25 @@ static __device__ void sample_p(const Ctx& x, ChainState& st, double* p) {
   st.nn += x.cfg.D;
 }
 
-static __device__ void copy_vec(const Ctx& x, double* dst, const double* src) {
+static __device__ void copy_vec(const Ctx& x, double* __restrict__ dst,
+                                const double* __restrict__ src) {
+#pragma unroll 4
   for (int i = x.lane; i < x.cfg.D; i += 32) dst[i] = src[i];
 }
 
 // begin_update_p / end_update_p: p -= (eps/2) g  (expl_leapfrog.hpp:16-28)
-static __device__ void half_kick(const Ctx& x, double* p, const double* g, double half) {
+static __device__ void half_kick(const Ctx& x, double* __restrict__ p,
+                                 const double* __restrict__ g, double half) {
+#pragma unroll 4
   for (int i = x.lane; i < x.cfg.D; i += 32) p[i] = DSUB(p[i], DMUL(half, g[i]));
 }
 
 // update_q: q += eps * invM p, then request the gradient at q.
-static __device__ void drift_and_request(const Ctx& x, double* q, const double* p,
-                                         double eps, double* req) {
-  const double* im = x.slot(SL_INVM);
+static __device__ void drift_and_request(const Ctx& x, double* __restrict__ q,
+                                         const double* __restrict__ p, double eps,
+                                         double* __restrict__ req) {
+  const double* __restrict__ im = x.slot(SL_INVM);
+#pragma unroll 4
   for (int i = x.lane; i < x.cfg.D; i += 32) {
     double v = DADD(q[i], DMUL(eps, DMUL(im[i], p[i])));
     q[i] = v;
@@ -224,6 +231,108 @@ static __device__ int learn_variance(const Ctx& x, ChainState& st) {
   return 0;
 }
 
+// The vector pass of an inner merge: rho and the edge momentum of level l,
+// its proposal if the final subtree is selected, and the six U-turn dot
+// products (partial per lane).  Pointers of the two subtrees never alias.
+static __device__ __forceinline__ void merge_level_pass(
+    int D, int lane, double* __restrict__ IQ, double* __restrict__ IP, double* __restrict__ IG,
+    const double* __restrict__ IPB, double* __restrict__ IPE, double* __restrict__ IR,
+    const double* __restrict__ CQ, const double* __restrict__ CP, const double* __restrict__ CG,
+    const double* __restrict__ CPB, const double* __restrict__ CPE,
+    const double* __restrict__ CR, const double* __restrict__ im, bool sel_final,
+    double* dd) {
+  double d1a = 0, d1b = 0, d2a = 0, d2b = 0, d3a = 0, d3b = 0;
+#pragma unroll 2
+  for (int i = lane; i < D; i += 32) {
+    const double ipb = IPB[i], ipe = IPE[i], ir = IR[i];
+    const double cpb = CPB[i], cpe = CPE[i], cr = CR[i];
+    const double psb = DMUL(im[i], ipb);   // p_sharp_beg
+    const double pse = DMUL(im[i], cpe);   // p_sharp_end
+    const double psie = DMUL(im[i], ipe);  // p_sharp_init_end
+    const double psfb = DMUL(im[i], cpb);  // p_sharp_final_beg
+    const double rs = DADD(ir, cr);        // rho_init + rho_final
+    const double r2 = DADD(ir, cpb);       // rho_init + p_final_beg
+    const double r3 = DADD(cr, ipe);       // rho_final + p_init_end
+    d1a += pse * rs;
+    d1b += psb * rs;
+    d2a += psfb * r2;
+    d2b += psb * r2;
+    d3a += pse * r3;
+    d3b += psie * r3;
+    IR[i] = rs;
+    IPE[i] = cpe;
+    if (sel_final) {
+      IQ[i] = CQ[i];
+      IP[i] = CP[i];
+      IG[i] = CG[i];
+    }
+  }
+  dd[0] = d1a;
+  dd[1] = d1b;
+  dd[2] = d2a;
+  dd[3] = d2b;
+  dd[4] = d3a;
+  dd[5] = d3b;
+}
+
+// The vector pass of the top-level merge: trajectory rho and edge momenta,
+// the sample if selected, and the six U-turn dot products (partial per lane).
+static __device__ __forceinline__ void merge_top_pass(
+    int D, int lane, bool fwd, bool sel, double* __restrict__ RHO, double* __restrict__ PFF,
+    double* __restrict__ PFB, double* __restrict__ PBF, double* __restrict__ PBB,
+    double* __restrict__ SQ, double* __restrict__ SP, double* __restrict__ SG,
+    const double* __restrict__ CQ, const double* __restrict__ CP, const double* __restrict__ CG,
+    const double* __restrict__ CPB, const double* __restrict__ CPE,
+    const double* __restrict__ CR, const double* __restrict__ im, double* dd) {
+  double d1a = 0, d1b = 0, d2a = 0, d2b = 0, d3a = 0, d3b = 0;
+#pragma unroll 2
+  for (int i = lane; i < D; i += 32) {
+    double rho_bck, rho_fwd, p_ff, p_fb, p_bf, p_bb;
+    if (fwd) {
+      rho_bck = RHO[i];
+      rho_fwd = CR[i];
+      p_bf = PFF[i];
+      p_fb = CPB[i];
+      p_ff = CPE[i];
+      p_bb = PBB[i];
+    } else {
+      rho_fwd = RHO[i];
+      rho_bck = CR[i];
+      p_fb = PBB[i];
+      p_bf = CPB[i];
+      p_bb = CPE[i];
+      p_ff = PFF[i];
+    }
+    const double rho = DADD(rho_bck, rho_fwd);
+    const double ps_bb = DMUL(im[i], p_bb), ps_ff = DMUL(im[i], p_ff);
+    const double ps_fb = DMUL(im[i], p_fb), ps_bf = DMUL(im[i], p_bf);
+    const double r2 = DADD(rho_bck, p_fb);
+    const double r3 = DADD(rho_fwd, p_bf);
+    d1a += ps_ff * rho;
+    d1b += ps_bb * rho;
+    d2a += ps_fb * r2;
+    d2b += ps_bb * r2;
+    d3a += ps_ff * r3;
+    d3b += ps_bf * r3;
+    RHO[i] = rho;
+    PFF[i] = p_ff;
+    PFB[i] = p_fb;
+    PBF[i] = p_bf;
+    PBB[i] = p_bb;
+    if (sel) {
+      SQ[i] = CQ[i];
+      SP[i] = CP[i];
+      SG[i] = CG[i];
+    }
+  }
+  dd[0] = d1a;
+  dd[1] = d1b;
+  dd[2] = d2a;
+  dd[3] = d2b;
+  dd[4] = d3a;
+  dd[5] = d3b;
+}
+
 // ---------------------------------------------------------------- the machine
 // Merges the subtree `cur` (the working leaf, or stack level cur_level) into
 // stack level l (its left sibling), as build_tree does after its final
@@ -266,32 +375,10 @@ static __device__ bool merge_into_level(const Ctx& x, ChainState& st, const Stk&
     double accept_prob = exp(cur_lsw - lsw_sub);
     sel_final = draw_uniform(cfg, st, x.c) < accept_prob;
   }
-  const double* im = x.slot(SL_INVM);
-  double d1a = 0, d1b = 0, d2a = 0, d2b = 0, d3a = 0, d3b = 0;
-  for (int i = x.lane; i < cfg.D; i += 32) {
-    const double ipb = IPB[i], ipe = IPE[i], ir = IR[i];
-    const double cpb = CPB[i], cpe = CPE[i], cr = CR[i];
-    const double psb = DMUL(im[i], ipb);   // p_sharp_beg
-    const double pse = DMUL(im[i], cpe);   // p_sharp_end
-    const double psie = DMUL(im[i], ipe);  // p_sharp_init_end
-    const double psfb = DMUL(im[i], cpb);  // p_sharp_final_beg
-    const double rs = DADD(ir, cr);        // rho_init + rho_final
-    const double r2 = DADD(ir, cpb);       // rho_init + p_final_beg
-    const double r3 = DADD(cr, ipe);       // rho_final + p_init_end
-    d1a += pse * rs;
-    d1b += psb * rs;
-    d2a += psfb * r2;
-    d2b += psb * r2;
-    d3a += pse * r3;
-    d3b += psie * r3;
-    IR[i] = rs;
-    IPE[i] = cpe;
-    if (sel_final) {
-      IQ[i] = CQ[i];
-      IP[i] = CP[i];
-      IG[i] = CG[i];
-    }
-  }
+  double dd[6];
+  merge_level_pass(cfg.D, x.lane, IQ, IP, IG, IPB, IPE, IR, CQ, CP, CG, CPB, CPE, CR,
+                   x.slot(SL_INVM), sel_final, dd);
+  double d1a = dd[0], d1b = dd[1], d2a = dd[2], d2b = dd[3], d3a = dd[4], d3b = dd[5];
   d1a = warp_sum(d1a);
   d1b = warp_sum(d1b);
   d2a = warp_sum(d2a);
@@ -345,46 +432,10 @@ static __device__ bool merge_top(const Ctx& x, ChainState& st, const Stk& sk, in
   double* SG = x.slot(SL_SMP_G);
   const double* im = x.slot(SL_INVM);
   const bool fwd = st.dir > 0;
-  double d1a = 0, d1b = 0, d2a = 0, d2b = 0, d3a = 0, d3b = 0;
-  for (int i = x.lane; i < cfg.D; i += 32) {
-    double rho_bck, rho_fwd, p_ff, p_fb, p_bf, p_bb;
-    if (fwd) {
-      rho_bck = RHO[i];
-      rho_fwd = CR[i];
-      p_bf = PFF[i];
-      p_fb = CPB[i];
-      p_ff = CPE[i];
-      p_bb = PBB[i];
-    } else {
-      rho_fwd = RHO[i];
-      rho_bck = CR[i];
-      p_fb = PBB[i];
-      p_bf = CPB[i];
-      p_bb = CPE[i];
-      p_ff = PFF[i];
-    }
-    const double rho = DADD(rho_bck, rho_fwd);
-    const double ps_bb = DMUL(im[i], p_bb), ps_ff = DMUL(im[i], p_ff);
-    const double ps_fb = DMUL(im[i], p_fb), ps_bf = DMUL(im[i], p_bf);
-    const double r2 = DADD(rho_bck, p_fb);
-    const double r3 = DADD(rho_fwd, p_bf);
-    d1a += ps_ff * rho;
-    d1b += ps_bb * rho;
-    d2a += ps_fb * r2;
-    d2b += ps_bb * r2;
-    d3a += ps_ff * r3;
-    d3b += ps_bf * r3;
-    RHO[i] = rho;
-    PFF[i] = p_ff;
-    PFB[i] = p_fb;
-    PBF[i] = p_bf;
-    PBB[i] = p_bb;
-    if (sel) {
-      SQ[i] = CQ[i];
-      SP[i] = CP[i];
-      SG[i] = CG[i];
-    }
-  }
+  double dd[6];
+  merge_top_pass(cfg.D, x.lane, fwd, sel, RHO, PFF, PFB, PBF, PBB, SQ, SP, SG, CQ, CP, CG, CPB,
+                 CPE, CR, im, dd);
+  double d1a = dd[0], d1b = dd[1], d2a = dd[2], d2b = dd[3], d3a = dd[4], d3b = dd[5];
   if (sel) st.V_smp = cur_V;
   d1a = warp_sum(d1a);
   d1b = warp_sum(d1b);
@@ -437,7 +488,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
   const int D = cfg.D;
   double* rq = req + (size_t)c * cfg.ld;
   const double inf = __longlong_as_double(0x7ff0000000000000LL);
-  const double log08 = log(0.8);
+  const double log08 = -0.22314355131420976;  // log(0.8)
   bool yield = false;
   int guard = 0;
   // The gradient requested at the previous yield, finalised from the split
