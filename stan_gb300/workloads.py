@@ -138,6 +138,39 @@ def hier_logistic(N=2000, K=8, seed=1, x_dtype="f32", name=None):
                    hp=(2.5, 1.0, 2.5), truth=truth)
 
 
+def hier_logistic_prior(N=2000, K=8, seed=1, name=None):
+    """Hierarchical logistic data simulated at a draw from the model's own
+    prior (alpha ~ N(0, 2.5), tau ~ half-N(0, 1), z ~ N(0, 1), beta ~ N(0, 2.5)),
+    J = N / 50 groups, X ~ N(0, 1) stored FP32: the serving stream's fits."""
+    rng = np.random.default_rng(seed)
+    J = max(1, N // 50)
+    sizes = np.full(J, N // J)
+    sizes[: N - sizes.sum()] += 1
+    g = np.repeat(np.arange(J, dtype=np.int32), sizes)
+    X = rng.normal(size=(N, K)).astype(np.float32).astype(np.float64)
+    alpha = rng.normal(scale=2.5)
+    tau = abs(rng.normal())
+    z = rng.normal(size=J)
+    beta = rng.normal(scale=2.5, size=K)
+    eta = alpha + tau * z[g] + X @ beta
+    y = (rng.random(N) < 1 / (1 + np.exp(-eta))).astype(np.float64)
+    truth = np.concatenate([[alpha, math.log(tau)], z, beta])
+    return Dataset(name or f"hier_logistic_prior_N{N}_K{K}", HIER_LOGISTIC, X, y, "f32", group=g,
+                   J=J, hp=(2.5, 1.0, 2.5), truth=truth)
+
+
+def serving_stream(n, seed=0):
+    """n serving fits: N log-uniform in [200, 50000], K uniform in {8, 16, 32,
+    64, 128}, data at prior draws (hier_logistic_prior)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        N = int(round(math.exp(rng.uniform(math.log(200), math.log(50000)))))
+        K = int(rng.choice([8, 16, 32, 64, 128]))
+        out.append(hier_logistic_prior(N, K, seed=1000 + 7919 * seed + i))
+    return out
+
+
 def make_dataset(kind, small=False, seed=1):
     """The workload datasets; small=True gives a same-shaped reduced case."""
     if kind == "logistic":
