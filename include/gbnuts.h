@@ -57,8 +57,12 @@ enum { GBNUTS_F64 = 0, GBNUTS_F32 = 1, GBNUTS_BF16 = 2 };
  *           does in double precision.
  *  BF16X3 : X.B and X^T.R as bf16 hi/lo split products on the tcgen05 tensor
  *           cores with FP32 accumulation (three products per contraction),
- *           totals and sampler state in double precision. */
-enum { GBNUTS_PREC_FP64 = 0, GBNUTS_PREC_FP32 = 1, GBNUTS_PREC_BF16X3 = 2 };
+ *           totals and sampler state in double precision.
+ *  BF16   : the same contractions as single bf16 products (no lo parts).
+ *  The bf16 forms take the logistic and Poisson GLMs: up to 127 features on
+ *  the tensor-memory kernel, wider designs as bf16 GEMMs around a link
+ *  kernel. */
+enum { GBNUTS_PREC_FP64 = 0, GBNUTS_PREC_FP32 = 1, GBNUTS_PREC_BF16X3 = 2, GBNUTS_PREC_BF16 = 3 };
 
 typedef struct gbnuts_model gbnuts_model;
 

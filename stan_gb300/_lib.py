@@ -12,8 +12,8 @@ LIB_PATH = os.path.join(_HERE, "_build", "libgbnuts.so")
 OK, USAGE, DATAERR, NOINPUT, SOFTWARE, CONFIG = 0, 64, 65, 66, 70, 78
 LOGISTIC, POISSON, HIER_NORMAL, HIER_LOGISTIC = 1, 2, 3, 4
 F64, F32, BF16 = 0, 1, 2
-PREC_FP64, PREC_FP32, PREC_BF16X3 = 0, 1, 2
-PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "bf16x3": PREC_BF16X3}
+PREC_FP64, PREC_FP32, PREC_BF16X3, PREC_BF16 = 0, 1, 2, 3
+PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "bf16x3": PREC_BF16X3, "bf16": PREC_BF16}
 INIT_WRITER, SAMPLE_WRITER, DIAGNOSTIC_WRITER = 0, 1, 2
 CHAIN_STATUS = {0: "ok", 1: "init_failed", 2: "stepsize_init_failed", 3: "stepsize_failed",
                 4: "metric_overflow", 5: "interrupted", 6: "bad_metric"}

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgbnuts.so")
-SOURCES = ["loglik.cu", "nuts.cu", "capi.cu", "glm_tc.cu", "noalloc.cu", "pool.cu", "glm_tct.cu"]
+SOURCES = ["loglik.cu", "nuts.cu", "capi.cu", "glm_tc.cu", "noalloc.cu", "pool.cu", "glm_tct.cu", "glm_gemm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -60,7 +60,7 @@ def build(verbose=False, force=False):
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart"]
+    cmd = [nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcublas", "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -34,12 +34,22 @@ using namespace gbn;
 
 // Builds the tensor-core tiles of X on first use of the bf16x3 form.
 static int ensure_precision(gbnuts_model* m, int precision) {
-  if (precision < GBNUTS_PREC_FP64 || precision > GBNUTS_PREC_BF16X3)
+  if (precision < GBNUTS_PREC_FP64 || precision > GBNUTS_PREC_BF16)
     return fail(GBNUTS_USAGE, "unknown precision");
-  if (precision != GBNUTS_PREC_BF16X3) return GBNUTS_OK;
+  if (!is_tensor_precision(precision)) return GBNUTS_OK;
+  if (!tc_supported(m->desc) && tensor_form_supported(m->desc)) {
+    // wide design: bf16 copies of X for the GEMM form
+    if (m->d_gx_h) return GBNUTS_OK;
+    int rc = gemm_prepare(m->desc, &m->d_gx_h, &m->d_gx_l, m->stream);
+    if (rc) return rc;
+    GBN_CUDA_TRY(cudaStreamSynchronize(m->stream));
+    m->desc.gx_h = m->d_gx_h;
+    m->desc.gx_l = m->d_gx_l;
+    return GBNUTS_OK;
+  }
   if (!tc_supported(m->desc))
     return fail(GBNUTS_USAGE,
-                "bf16x3 precision needs a logistic or Poisson GLM with K + intercept <= 128");
+                "the bf16 tensor-core forms need a logistic or Poisson GLM");
   if (m->d_tc_xt) return GBNUTS_OK;
   int tiles = 0;
   int rc = tc_prepare(m->desc, &m->d_tc_xt, &m->d_tc_yt, &tiles, m->stream);
@@ -259,6 +269,8 @@ void gbnuts_model_destroy(gbnuts_model* m) {
   free_workspace(m->ws);
   if (m->d_tc_xt) cudaFree(m->d_tc_xt);
   if (m->d_tc_yt) cudaFree(m->d_tc_yt);
+  if (m->d_gx_h) cudaFree(m->d_gx_h);
+  if (m->d_gx_l) cudaFree(m->d_gx_l);
   if (m->d_theta) cudaFree(m->d_theta);
   if (m->d_X) cudaFree(m->d_X);
   if (m->d_y) cudaFree(m->d_y);
@@ -582,7 +594,7 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   GBN_CUDA_TRY(dr.alloc(&d_cmap, C));
   GBN_CUDA_TRY(cudaMemcpyAsync(d_fit, &h_fit, sizeof(h_fit), cudaMemcpyHostToDevice, st));
   GBN_CUDA_TRY(cudaMemcpyAsync(d_cmap, h_cmap.data(), C * sizeof(int2), cudaMemcpyHostToDevice, st));
-  const bool pool_partials = rc->precision != GBNUTS_PREC_BF16X3 && chains_per_block(m->desc.K) == 16;
+  const bool pool_partials = !is_tensor_precision(rc->precision) && chains_per_block(m->desc.K) == 16;
   PoolGradFit* d_gfit = nullptr;
   PoolWorkItem* d_items = nullptr;
   int n_items = 0;

@@ -30,6 +30,8 @@ struct gbnuts_model {
   cudaStream_t stream = nullptr;
   void* d_tc_xt = nullptr;
   float* d_tc_yt = nullptr;
+  void* d_gx_h = nullptr;
+  void* d_gx_l = nullptr;
 };
 
 

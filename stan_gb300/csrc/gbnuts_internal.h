@@ -49,6 +49,9 @@ struct ModelDesc {
   const void* tc_xt;
   const float* tc_yt;
   int tc_tiles;
+  // wide-design tensor-core form: X as row-major bf16 hi (and lo) copies
+  const void* gx_h;
+  const void* gx_l;
 };
 
 // Number of per-(split, chain) partial sums: lp, sum r, sum r z_g, sum e^2, beta[K].
@@ -62,6 +65,7 @@ struct GradWorkspace {
   long long* split_rows = nullptr;  // [S+1] device
   int* err = nullptr;               // device error flag of bounded waits
   int precision = -1;
+  void* gemm = nullptr;  // buffers of the wide-design tensor-core form
   std::vector<long long> h_split_rows;
   size_t bytes = 0;
 };
@@ -125,15 +129,26 @@ int launch_tc(const ModelDesc& m, const double* Q, int ldq, int C, const int* ac
               GradWorkspace& ws, cudaStream_t st);
 // Chains-on-M form (Theta and R as tensor-memory operands, 128 chains per CTA).
 int tct_splits(const ModelDesc& m, int C);
-int launch_tct(const ModelDesc& m, const double* Q, int ldq, int C, const int* active,
-               GradWorkspace& ws, cudaStream_t st);
+int launch_tct(const ModelDesc& m, int precision, const double* Q, int ldq, int C,
+               const int* active, GradWorkspace& ws, cudaStream_t st);
 // Which tensor-core kernel the bf16x3 form uses (GBNUTS_TC_KERNEL=m64 selects
 // the chains-on-N kernel, for comparisons).
 bool tc_chains_on_m();
-// Whether the model can use the tensor-core form.
+// Whether the model can use the tensor-memory kernel (K + intercept <= 128).
 inline bool tc_supported(const ModelDesc& m) {
   return (m.link == LINK_LOGIT || m.link == LINK_POISSON_LOG) && m.off_z < 0 &&
          m.K + m.has_base <= 128;
 }
+// Whether the model has a bf16 tensor-core form at all (GLM families).
+inline bool tensor_form_supported(const ModelDesc& m) {
+  return (m.link == LINK_LOGIT || m.link == LINK_POISSON_LOG) && m.off_z < 0;
+}
+inline bool is_tensor_precision(int p) { return p == 2 || p == 3; }
+// Wide-design form (glm_gemm.cu): bf16 GEMMs around a link kernel.
+int gemm_kpad(const ModelDesc& m);
+int gemm_prepare(const ModelDesc& m, void** xh, void** xl, cudaStream_t st);
+int launch_gemm(const ModelDesc& m, int precision, const double* Q, int ldq, int C,
+                const int* active, GradWorkspace& ws, cudaStream_t st);
+void gemm_free_work(GradWorkspace& ws);
 
 }  // namespace gbn

@@ -150,7 +150,9 @@ __device__ __forceinline__ void two_sum_add(float2& s, float v) {
   s.y += err;
 }
 
-template <int LINK, bool XLO>
+// SPLIT: the hi/lo split products (bf16x3); otherwise one bf16 product per
+// contraction (the plain bf16 form; X's lo part unused).
+template <int LINK, bool XLO, bool SPLIT>
 __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
   using namespace tct;
   extern __shared__ unsigned char smem_raw[];
@@ -198,7 +200,8 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
   const int t_begin = (int)((long long)a.n_tiles * s / a.S);
   const int t_end = (int)((long long)a.n_tiles * (s + 1) / a.S);
   const int n = t_end - t_begin;
-  const uint32_t x_bytes = XLO ? 2u * PART_BYTES : (uint32_t)PART_BYTES;
+  constexpr bool kXlo = XLO && SPLIT;
+  const uint32_t x_bytes = kXlo ? 2u * PART_BYTES : (uint32_t)PART_BYTES;
   const int ksteps = (Kx + 15) / 16;   // GEMM1 contraction steps holding features
   const int nf = 16 * ksteps;          // GEMM2 N: features rounded up to 16
 
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
           const __nv_bfloat16* src = a.xt + (size_t)(2 * (t_begin + i)) * (TM * TK);
           mbar_arrive_expect_tx(&bars[B_XFULL + st], x_bytes + Y_BYTES);
           bulk_copy_g2s(dst, src, PART_BYTES, &bars[B_XFULL + st]);
-          if (XLO)
+          if (kXlo)
             bulk_copy_g2s(dst + PART_BYTES, src + TM * TK, PART_BYTES, &bars[B_XFULL + st]);
           bulk_copy_g2s(dst + 2 * PART_BYTES, a.yt + (size_t)(t_begin + i) * TM, Y_BYTES,
                         &bars[B_XFULL + st]);
@@ -238,8 +241,8 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
             const uint64_t bh = desc_feats(xh, ks);
             mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RH + 8 * ks, bh, id2,
                             (i > 0 || ks > 0) ? 1u : 0u);
-            mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RL + 8 * ks, bh, id2, 1u);
-            if (XLO) mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RH + 8 * ks, desc_feats(xl, ks), id2, 1u);
+            if (SPLIT) mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RL + 8 * ks, bh, id2, 1u);
+            if (kXlo) mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RH + 8 * ks, desc_feats(xl, ks), id2, 1u);
           }
           mma_commit(&bars[B_REMPTY]);
           mma_commit(&bars[B_XEMPTY + st]);
@@ -257,8 +260,8 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
           for (int ks = 0; ks < ksteps; ++ks) {
             const uint64_t bh = desc_rows(xh, ks);
             mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TH + 8 * ks, bh, id1, ks > 0 ? 1u : 0u);
-            mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TL + 8 * ks, bh, id1, 1u);
-            if (XLO) mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TH + 8 * ks, desc_rows(xl, ks), id1, 1u);
+            if (SPLIT) mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TL + 8 * ks, bh, id1, 1u);
+            if (kXlo) mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TH + 8 * ks, desc_rows(xl, ks), id1, 1u);
           }
           mma_commit(&bars[B_D1FULL]);
           if (i > 0) ok = gemm2(i - 1);
@@ -392,21 +395,23 @@ int tct_splits(const ModelDesc& m, int C) {
   return S;
 }
 
-int launch_tct(const ModelDesc& m, const double* Q, int ldq, int C, const int* active,
-               GradWorkspace& ws, cudaStream_t st) {
+template <int LINK, bool XLO, bool SPLIT>
+static int launch_tct_t(const TctArgs& a, dim3 grid, cudaStream_t st) {
   using namespace tct;
   static bool attr = false;
   if (!attr) {
-    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tct_kernel<LINK_LOGIT, true>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
-    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tct_kernel<LINK_LOGIT, false>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
-    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tct_kernel<LINK_POISSON_LOG, true>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
-    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tct_kernel<LINK_POISSON_LOG, false>,
+    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tct_kernel<LINK, XLO, SPLIT>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
     attr = true;
   }
+  glm_tct_kernel<LINK, XLO, SPLIT><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
+  GBN_CUDA_TRY(cudaGetLastError());
+  return GBNUTS_OK;
+}
+
+int launch_tct(const ModelDesc& m, int precision, const double* Q, int ldq, int C,
+               const int* active, GradWorkspace& ws, cudaStream_t st) {
+  using namespace tct;
   TctArgs a;
   a.xt = static_cast<const __nv_bfloat16*>(m.tc_xt);
   a.yt = m.tc_yt;
@@ -423,20 +428,16 @@ int launch_tct(const ModelDesc& m, const double* Q, int ldq, int C, const int* a
   a.S = ws.S;
   a.err = ws.err;
   const bool xlo = m.x_dtype != GBNUTS_BF16;
+  const bool split = precision == GBNUTS_PREC_BF16X3;
   dim3 grid(ws.S, (C + NCH - 1) / NCH);
   if (m.link == LINK_LOGIT) {
-    if (xlo)
-      glm_tct_kernel<LINK_LOGIT, true><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
-    else
-      glm_tct_kernel<LINK_LOGIT, false><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
-  } else {
-    if (xlo)
-      glm_tct_kernel<LINK_POISSON_LOG, true><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
-    else
-      glm_tct_kernel<LINK_POISSON_LOG, false><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
+    if (!split) return launch_tct_t<LINK_LOGIT, false, false>(a, grid, st);
+    return xlo ? launch_tct_t<LINK_LOGIT, true, true>(a, grid, st)
+               : launch_tct_t<LINK_LOGIT, false, true>(a, grid, st);
   }
-  GBN_CUDA_TRY(cudaGetLastError());
-  return GBNUTS_OK;
+  if (!split) return launch_tct_t<LINK_POISSON_LOG, false, false>(a, grid, st);
+  return xlo ? launch_tct_t<LINK_POISSON_LOG, true, true>(a, grid, st)
+             : launch_tct_t<LINK_POISSON_LOG, false, true>(a, grid, st);
 }
 
 // ------------------------------------------------------------------ probe

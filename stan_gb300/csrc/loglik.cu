@@ -438,7 +438,10 @@ static long long split_rows_min() {
 }
 
 int choose_splits(const ModelDesc& m, int C, int precision) {
-  if (precision == GBNUTS_PREC_BF16X3) return tc_chains_on_m() ? tct_splits(m, C) : tc_splits(m, C);
+  if (is_tensor_precision(precision)) {
+    if (!tc_supported(m)) return 1;  // wide-design GEMM form: one partial row per chain
+    return tc_chains_on_m() ? tct_splits(m, C) : tc_splits(m, C);
+  }
   const int CB = chains_per_block(m.K);
   const int chain_blocks = (C + CB - 1) / CB;
   // Splits: enough CTAs for ~2 waves over 152 SMs, a minimum of rows each.
@@ -455,8 +458,8 @@ int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int pre
     set_last_error("K beyond the supported maximum (2048)");
     return GBNUTS_USAGE;
   }
-  if (precision == GBNUTS_PREC_BF16X3 && !tc_supported(m)) {
-    set_last_error("bf16x3 precision needs a logistic or Poisson GLM with K + intercept <= 128");
+  if (is_tensor_precision(precision) && !tensor_form_supported(m)) {
+    set_last_error("the bf16 tensor-core forms need a logistic or Poisson GLM");
     return GBNUTS_USAGE;
   }
   const int S = choose_splits(m, C, precision);
@@ -500,6 +503,7 @@ int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int pre
 
 void free_workspace(GradWorkspace& ws) {
   if (ws.partial) cudaFree(ws.partial);
+  gemm_free_work(ws);
   ws = GradWorkspace();
 }
 
@@ -513,9 +517,13 @@ int launch_partials(const ModelDesc& m, int precision, const double* Q, int ldq,
     dispatch_x<double>(m, Q, ldq, C, active, ws, stream);
   } else if (precision == GBNUTS_PREC_FP32) {
     dispatch_x<float>(m, Q, ldq, C, active, ws, stream);
-  } else if (precision == GBNUTS_PREC_BF16X3 && m.tc_xt != nullptr) {
-    int rc = tc_chains_on_m() ? launch_tct(m, Q, ldq, C, active, ws, stream)
-                              : launch_tc(m, Q, ldq, C, active, ws, stream);
+  } else if (is_tensor_precision(precision) && m.tc_xt != nullptr) {
+    int rc = (tc_chains_on_m() || precision == GBNUTS_PREC_BF16)
+                 ? launch_tct(m, precision, Q, ldq, C, active, ws, stream)
+                 : launch_tc(m, Q, ldq, C, active, ws, stream);
+    if (rc) return rc;
+  } else if (is_tensor_precision(precision) && m.gx_h != nullptr) {
+    int rc = launch_gemm(m, precision, Q, ldq, C, active, ws, stream);
     if (rc) return rc;
   } else {
     set_last_error("precision not available for this model");

@@ -123,3 +123,46 @@ def test_bf16x3_posterior_matches_fp64_within_mcse():
     for j in range(m.D):
         se = np.hypot(analyze.mcse_mean(d64[:, :, j]), analyze.mcse_mean(dmx[:, :, j]))
         assert abs(d64[:, :, j].mean() - dmx[:, :, j].mean()) <= 4 * se, j
+
+
+def _errors(m, om, th, precision):
+    lp, g = m.log_prob_grad_batch(th, precision)
+    e_lp, e_g = 0.0, 0.0
+    for c in range(th.shape[0]):
+        lpo, go = om.log_prob_grad(th[c])
+        e_lp = max(e_lp, abs(lp[c] - lpo) / abs(lpo))
+        e_g = max(e_g, np.linalg.norm(g[c] - go) / np.linalg.norm(go))
+    return e_lp, e_g
+
+
+@pytest.mark.parametrize("case", ["poisson_k512_bf16x", "logistic_k200_f32x"])
+def test_wide_design_bf16_forms_match_fp64_oracle(case):
+    """K + intercept > 127: the bf16 GEMM form.  Split (bf16x3): lp within 1e-5,
+    gradient within 1e-4 of the FP64 oracle; plain bf16: within 2e-2."""
+    from stan_gb300 import Model, workloads
+    if case == "poisson_k512_bf16x":
+        ds = workloads.poisson(4096, 512, seed=3, x_dtype="bf16")
+    else:
+        ds = workloads.logistic(3000, 200, seed=4, x_dtype="f32", standardise=True)
+    m = Model.from_dataset(ds)
+    om = ds.oracle_model()
+    C = 130  # two chain blocks of 128, the second mostly empty
+    th = np.random.default_rng(6).normal(size=(C, m.D)) * (0.5 / np.sqrt(ds.K))
+    e_lp, e_g = _errors(m, om, th, "bf16x3")
+    assert e_lp <= 1e-5 and e_g <= 1e-4, (e_lp, e_g)
+    e_lp, e_g = _errors(m, om, th, "bf16")
+    assert e_lp <= 2e-2 and e_g <= 2e-2, (e_lp, e_g)
+
+
+def test_plain_bf16_tensor_memory_kernel():
+    """The plain bf16 form on the tensor-memory kernel (K + intercept <= 127)."""
+    from stan_gb300 import Model
+    ds = make_dataset("logistic_100k", small=True, seed=9)
+    m = Model.from_dataset(ds)
+    om = ds.oracle_model()
+    th = np.random.default_rng(7).normal(size=(70, m.D)) * 0.3
+    e_lp, e_g = _errors(m, om, th, "bf16")
+    assert e_lp <= 2e-2 and e_g <= 2e-2, (e_lp, e_g)
+    # the split form is far closer on the same points
+    e_lp3, e_g3 = _errors(m, om, th, "bf16x3")
+    assert e_g3 < e_g
