@@ -239,6 +239,11 @@ def run_ours(args, ws, rank, local):
             "min_bulk_ess_per_s_estimate"]
         if args.precision != "fp64":
             out["precision_errors"] = precision_errors(model, last, args.precision)
+    if rank == 0 and not args.no_config_d:
+        try:
+            out["config_d"] = config_d_leg()
+        except Exception as e:  # reported, not fatal to the headline line
+            out["config_d"] = {"error": repr(e)}
     if rank == 0 and not args.no_serving:
         try:
             out["serving"] = serving_leg()
@@ -288,6 +293,34 @@ def precision_errors(model, res, precision, n_theta=64):
             "lp_max_rel": float(lp_rel.max()), "grad_max_rel": float(g_rel.max()),
             "energy_abs_diff": {"n": int(C), "median": float(np.median(dh)),
                                 "p99": float(np.percentile(dh, 99)), "max": float(dh.max())}}
+
+
+def config_d_leg():
+    """Poisson GLM, N = 262144, K = 512, X stored bf16, 512 chains: gradient
+    time of each form inside a short fit (CUDA events), and the mixed forms'
+    errors against the FP64 form at 64 seeded points."""
+    from stan_gb300 import Model, sampler, workloads
+    ds = workloads.make_dataset("poisson", seed=1)
+    m = Model.from_dataset(ds)
+    C = 512
+    out = {"workload": "Poisson GLM N=262144 K=512, X bf16, 512 chains",
+           "flops_per_grad": 4.0 * ds.N * ds.K * C}
+    for prec in ("bf16x3", "bf16", "fp32"):
+        sampler.run(m, num_chains=C, num_warmup=4, num_samples=0, precision=prec,
+                    random_seed=1, init_radius=0.5)
+        r = sampler.run(m, num_chains=C, num_warmup=10, num_samples=0, precision=prec,
+                        random_seed=2, init_radius=0.5)
+        out[prec] = {"grad_ms": r.grad_ms,
+                     "tflops": out["flops_per_grad"] / (r.grad_ms * 1e-3) / 1e12}
+    th = np.random.default_rng(3).normal(size=(64, m.D)) * 0.05
+    lp64, g64 = m.log_prob_grad_batch(th, "fp64")
+    for prec in ("bf16x3", "bf16", "fp32"):
+        lp, g = m.log_prob_grad_batch(th, prec)
+        out[prec]["lp_max_rel"] = float(np.max(np.abs(lp - lp64) / np.abs(lp64)))
+        out[prec]["grad_max_rel"] = float(np.max(np.linalg.norm(g - g64, axis=1) /
+                                                 np.linalg.norm(g64, axis=1)))
+    m.close()
+    return out
 
 
 def fp64_rate(model, ds, C):
@@ -428,6 +461,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-config-d", action="store_true")
     ap.add_argument("--serving-fits", type=int, default=None)
     ap.add_argument("--serving-rate", type=float, default=None)
     ap.add_argument("--case", default="fit", choices=["fit", "grad", "shortfit", "serving"],
