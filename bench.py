@@ -206,7 +206,10 @@ def run_ours(args, ws, rank, local):
     kpad = 16 * ((K + 1 + 15) // 16)
     executed = 3 * 2 * 2.0 * N * C * kpad  # three bf16 products, two contractions, K padded
     roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-            "frac": ach / peak, "traffic": None,
+            "frac": ach / peak,
+            # dram__bytes_read.sum + dram__bytes_write.sum of one launch
+            # (profiles/glm_tct_kernel_logistic_100k_1024chains.md)
+            "traffic": 5.70e7 if args.precision == "bf16x3" else None,
             "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)",
             "kernel": "glm_tct_kernel" if args.precision == "bf16x3" else "loglik_partial_pool_kernel",
             "executed_tflops": executed / (mean_ms * 1e-3) / 1e12,
