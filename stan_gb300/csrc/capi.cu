@@ -23,6 +23,7 @@
 #include "gbnuts_internal.h"
 #include "nuts_device.h"
 #include "capi_internal.h"
+#include "tc_common.cuh"
 
 namespace gbn {
 static thread_local std::string g_last_error;
@@ -586,6 +587,21 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   h_fit.m = m->desc;
   h_fit.f = FitPtrs{d_states, d_stacks, d_vecs, d_req, pv, d_active, d_draws,
                     d_diag, d_init, d_inits, d_done, d_abort};
+  // the tensor-memory gradient kernel reads the request as packed words
+  uint32_t* d_reqw = nullptr;
+  struct WordsGuard {
+    GradWorkspace* ws = nullptr;
+    ~WordsGuard() {
+      if (ws) ws->tc_words = nullptr;
+    }
+  } words_guard;
+  if (is_tensor_precision(rc->precision) && m->desc.tc_xt &&
+      (tc_chains_on_m() || rc->precision == GBNUTS_PREC_BF16)) {
+    GBN_CUDA_TRY(dr.alloc(&d_reqw, (size_t)C * tc::kThetaWords));
+    h_fit.f.req_tc = d_reqw;
+    m->ws.tc_words = d_reqw;
+    words_guard.ws = &m->ws;
+  }
   std::vector<int2> h_cmap(C);
   for (int c = 0; c < C; ++c) h_cmap[c] = make_int2(0, c);
   PoolFitDev* d_fit;

@@ -66,6 +66,9 @@ struct GradWorkspace {
   int* err = nullptr;               // device error flag of bounded waits
   int precision = -1;
   void* gemm = nullptr;  // buffers of the wide-design tensor-core form
+  // theta of the current request as tensor-core words, written by the step
+  // kernel during a sampler run (null otherwise)
+  const uint32_t* tc_words = nullptr;
   std::vector<long long> h_split_rows;
   size_t bytes = 0;
 };

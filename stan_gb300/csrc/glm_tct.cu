@@ -52,7 +52,6 @@ constexpr int SMEM_X = 0;
 constexpr int SMEM_LP = SMEM_X + STAGES * STAGE_BYTES;   // [EPI_SUB][NCH] doubles
 constexpr int SMEM_BAR = SMEM_LP + EPI_SUB * NCH * 8;
 constexpr double kLn2 = 0.69314718055994530942;
-constexpr float kLog2ef = 1.44269504f;
 constexpr int SMEM_TOTAL = SMEM_BAR + 256;
 constexpr int SMEM_ALLOC = SMEM_TOTAL + 1024;  // slack for 1 KiB alignment
 // TMEM column map
@@ -77,6 +76,7 @@ struct TctArgs {
   long long N;
   int K, has_base, n_tiles;
   const double* Q;
+  const uint32_t* QW;  // theta as packed words (kThetaWords per chain), or null
   int ldq, C;
   const int* active;
   double* P;
@@ -283,19 +283,27 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
       {
         const bool act = act_s[c] != 0;
         const double* th = a.Q + (size_t)(act ? c0 + c : 0) * a.ldq;
+        const uint32_t* tw = a.QW ? a.QW + (size_t)(act ? c0 + c : 0) * kThetaWords : nullptr;
 #pragma unroll
         for (int part = 0; part < FW / 32; ++part) {
           uint32_t wh[16], wl[16];
+          const int w0 = FW / 2 * sub + 16 * part;
+          if (tw && act) {
+            // words written by the step kernel with the request (vector loads)
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int k = FW * sub + 32 * part + 2 * j;
-            const float f0 = (act && k < Kx) ? (float)th[k] * kLog2ef : 0.f;
-            const float f1 = (act && k + 1 < Kx) ? (float)th[k + 1] * kLog2ef : 0.f;
-            const __nv_bfloat162 hp = __floats2bfloat162_rn(f0, f1);
-            const float2 hf = __bfloat1622float2(hp);
-            const __nv_bfloat162 lo = __floats2bfloat162_rn(f0 - hf.x, f1 - hf.y);
-            wh[j] = *reinterpret_cast<const uint32_t*>(&hp);
-            wl[j] = *reinterpret_cast<const uint32_t*>(&lo);
+            for (int j = 0; j < 16; j += 4) {
+              const uint4 h4 = *reinterpret_cast<const uint4*>(tw + w0 + j);
+              const uint4 l4 = *reinterpret_cast<const uint4*>(tw + 64 + w0 + j);
+              wh[j] = h4.x; wh[j + 1] = h4.y; wh[j + 2] = h4.z; wh[j + 3] = h4.w;
+              wl[j] = l4.x; wl[j + 1] = l4.y; wl[j + 2] = l4.z; wl[j + 3] = l4.w;
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int k = FW * sub + 32 * part + 2 * j;
+              theta_words((act && k < Kx) ? th[k] : 0.0, (act && k + 1 < Kx) ? th[k + 1] : 0.0,
+                          wh[j], wl[j]);
+            }
           }
           tmem_st16(lane_addr + COL_TH + FW / 2 * sub + 16 * part, wh);
           tmem_st16(lane_addr + COL_TL + FW / 2 * sub + 16 * part, wl);
@@ -420,6 +428,7 @@ int launch_tct(const ModelDesc& m, int precision, const double* Q, int ldq, int 
   a.has_base = m.has_base;
   a.n_tiles = m.tc_tiles;
   a.Q = Q;
+  a.QW = ws.tc_words;
   a.ldq = ldq;
   a.C = C;
   a.active = active;

@@ -34,6 +34,7 @@
 #include "gbnuts_internal.h"
 #include "loglik_finalize.cuh"
 #include "nuts_device.h"
+#include "tc_common.cuh"
 
 namespace gbn {
 
@@ -126,6 +127,19 @@ static __device__ void drift_and_request(const Ctx& x, double* __restrict__ q,
     double v = DADD(q[i], DMUL(eps, DMUL(im[i], p[i])));
     q[i] = v;
     req[i] = v;
+  }
+}
+
+// The request as tensor-core coefficient words (features 0..127, zeros past
+// D), for the chains-on-M gradient kernel.  Reads back the warp's own writes.
+static __device__ void pack_request_words(const Ctx& x, const double* rq, uint32_t* w) {
+  __syncwarp();
+  for (int j = x.lane; j < tc::kThetaWords / 2; j += 32) {
+    const int k = 2 * j;
+    uint32_t wh, wl;
+    tc::theta_words(k < x.cfg.D ? rq[k] : 0.0, k + 1 < x.cfg.D ? rq[k + 1] : 0.0, wh, wl);
+    w[j] = wh;
+    w[tc::kThetaWords / 2 + j] = wl;
   }
 }
 
@@ -471,6 +485,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
   const double* __restrict__ inits = f.inits;
   int* __restrict__ done_count = f.done_count;
   const int* __restrict__ abort_flag = f.abort_flag;
+  uint32_t* req_tc = f.req_tc ? f.req_tc + (size_t)c * tc::kThetaWords : nullptr;
   ChainState st = states[c];
   if (st.done) {
     if (lane == 0) active[c] = 0;
@@ -525,6 +540,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
           rq[i] = v;
         }
         if (!inits && cfg.init_radius != 0.0) st.nu += D;
+        if (req_tc) pack_request_words(x, rq, req_tc);
         st.phase = PH_INIT_EVAL;
         yield = true;
         break;
@@ -581,6 +597,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         const double e = st.nom_eps;
         half_kick(x, p, g, 0.5 * e);
         drift_and_request(x, q, p, e, rq);
+        if (req_tc) pack_request_words(x, rq, req_tc);
         st.phase = PH_SS_EVAL;
         yield = true;
         break;
@@ -721,6 +738,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         const double e = st.dir * st.eps;
         half_kick(x, p, g, 0.5 * e);
         drift_and_request(x, q, p, e, rq);
+        if (req_tc) pack_request_words(x, rq, req_tc);
         st.phase = PH_LEAF_EVAL;
         yield = true;
         break;

@@ -90,6 +90,9 @@ struct FitPtrs {
   const double* inits;
   int* done_count;
   const int* abort_flag;
+  // the request also as chains-on-M tensor-core words (kThetaWords per chain),
+  // or null when the gradient form does not read them
+  uint32_t* req_tc;
 };
 
 void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* stacks,

@@ -263,6 +263,33 @@ __host__ __device__ __forceinline__ uint32_t kmajor_off(int r, int k, int kt) {
   return (uint32_t)((r >> 3) * (kt >> 3) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
 
+// double -> float rounded toward zero with integer operations only (the
+// FP64 pipe is slow on this part): sign, rebiased exponent, top 23 mantissa
+// bits; magnitudes below the float normal range give 0, above it infinity.
+__device__ __forceinline__ float dbl_to_flt_rz(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+  if (e <= 0) return __int_as_float((int)sign);
+  if (e >= 255) return __int_as_float((int)(sign | 0x7f800000u));
+  return __int_as_float((int)(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu)));
+}
+
+// Coefficient words of the chains-on-M tensor-core kernel: theta_k and
+// theta_{k+1} scaled by log2(e), split into bf16 hi and lo parts, packed two
+// per 32-bit word (element k in the low half).
+__device__ __forceinline__ void theta_words(double d0, double d1, uint32_t& wh, uint32_t& wl) {
+  const float f0 = dbl_to_flt_rz(d0) * 1.44269504f;
+  const float f1 = dbl_to_flt_rz(d1) * 1.44269504f;
+  const __nv_bfloat162 hp = __floats2bfloat162_rn(f0, f1);
+  const float2 hf = __bfloat1622float2(hp);
+  const __nv_bfloat162 lo = __floats2bfloat162_rn(f0 - hf.x, f1 - hf.y);
+  wh = *reinterpret_cast<const uint32_t*>(&hp);
+  wl = *reinterpret_cast<const uint32_t*>(&lo);
+}
+// Words per chain: 64 hi then 64 lo (128 features).
+constexpr int kThetaWords = 128;
+
 // bf16 hi/lo split of a value: hi = bf16(v), lo = bf16(v - hi).
 __device__ __forceinline__ void split_bf16(float v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
   hi = __float2bfloat16_rn(v);
