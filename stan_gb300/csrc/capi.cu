@@ -636,7 +636,7 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   // One step: every chain's state machine runs to its next gradient request,
   // then the gradient stage writes split partials the next step finalises.
   auto enqueue_step = [&](cudaEvent_t e0, cudaEvent_t e1) -> int {
-    launch_nuts_step_pool(d_fit, d_cmap, C, st);
+    launch_nuts_step_pool(d_fit, d_cmap, C, team_warps(D), st);
     if (!pool_partials)
       return launch_partials(m->desc, rc->precision, d_req, cfg.ld, C, d_active, m->ws, st, e0,
                              e1);

@@ -316,8 +316,9 @@ __global__ void __launch_bounds__(128)
   const int lane = threadIdx.x & 31;
   if (c >= C) return;  // uniform per warp
   if (active && !active[c]) return;
+  const Team tm{lane, 32, 1, nullptr};
   const double lp = finalize_chain(m, Q + (size_t)c * ldq, c, C, P, NP, S, Gz,
-                                   grad + (size_t)c * ldg, 1.0, propto, jacobian, lane,
+                                   grad + (size_t)c * ldg, 1.0, propto, jacobian, tm,
                                    sh_cs[threadIdx.x >> 5]);
   if (lane == 0) lp_out[c] = lp;
 }

@@ -1,7 +1,8 @@
 // Finalisation of one chain's log density and gradient from the split
 // partial sums: split sums in a fixed order (deterministic), priors, the
 // Jacobian of tau = exp(u), sigma = exp(u), and the chain rule through them.
-// One warp per chain, lanes over the coordinates; returns lp in every lane.
+// One team of threads per chain (team.cuh), threads over the coordinates;
+// returns lp in every thread.
 // The split sums go through a shared buffer first (split_column_sums).
 // Shared by the batched-gradient finalize kernel and the sampler step kernel.
 #pragma once
@@ -9,6 +10,7 @@
 #include <math.h>
 
 #include "gbnuts_internal.h"
+#include "team.cuh"
 
 namespace gbn {
 
@@ -25,10 +27,12 @@ static constexpr int kLanesOverSplits = 32;
 // split order, their loads issued eight at a time.  The order of additions
 // depends on S and NP only.
 __device__ __forceinline__ void split_column_sums(const double* __restrict__ Pc, size_t pstride,
-                                                  int S, int NP, double* cs, int lane) {
+                                                  int S, int NP, double* cs, const Team& tm) {
   if (S >= kLanesOverSplits) {
+    // each warp of the team takes every nw-th column
+    const int lane = tm.t & 31;
 #pragma unroll 4
-    for (int k = 0; k < NP; ++k) {
+    for (int k = tm.t >> 5; k < NP; k += tm.nw) {
       double a = 0;
       for (int s = lane; s < S; s += 32) a += Pc[s * pstride + k];
 #pragma unroll
@@ -36,8 +40,8 @@ __device__ __forceinline__ void split_column_sums(const double* __restrict__ Pc,
       if (lane == 0) cs[k] = a;
     }
   } else {
-    for (int kb = 0; kb < NP; kb += 32) {
-      const int k = kb + lane;
+    for (int kb = 0; kb < NP; kb += tm.n) {
+      const int k = kb + tm.t;
       double a = 0;
       for (int s0 = 0; s0 < S; s0 += 8) {
         double t[8];
@@ -51,20 +55,20 @@ __device__ __forceinline__ void split_column_sums(const double* __restrict__ Pc,
       if (k < NP) cs[k] = a;
     }
   }
-  __syncwarp();
+  tm.sync();
 }
 
 // th: the chain's parameters; grad_out[d] = sign * d lp / d theta_d.  cs: the
-// warp's shared buffer of kMaxColSums doubles.
+// team's shared buffer of kMaxColSums doubles.
 __device__ __forceinline__ double finalize_chain(const ModelDesc& m, const double* th, int c,
                                                  int C, const double* __restrict__ P, int NP,
                                                  int S, const double* __restrict__ Gz,
                                                  double* grad_out, double sign, int propto,
-                                                 int jacobian, int lane, double* cs) {
+                                                 int jacobian, const Team& tm, double* cs) {
   const size_t pstride = (size_t)C * NP;
   const double* Pc = P + (size_t)c * NP;
   const bool use_cs = NP <= kMaxColSums;
-  if (use_cs) split_column_sums(Pc, pstride, S, NP, cs, lane);
+  if (use_cs) split_column_sums(Pc, pstride, S, NP, cs, tm);
   // sum over splits of partial column k (split order when lanes run over columns)
   auto col = [&](int k) -> double {
     if (use_cs) return cs[k];
@@ -76,7 +80,7 @@ __device__ __forceinline__ double finalize_chain(const ModelDesc& m, const doubl
   const double tau = m.idx_tau >= 0 ? exp(th[m.idx_tau]) : 0.0;
   const double jac = jacobian ? 1.0 : 0.0;
   double prior = 0.0;
-  for (int d = lane; d < m.D; d += 32) {
+  for (int d = tm.t; d < m.D; d += tm.n) {
     const double t = th[d];
     double g;
     if (d >= m.off_beta) {
@@ -111,8 +115,7 @@ __device__ __forceinline__ double finalize_chain(const ModelDesc& m, const doubl
     }
     grad_out[d] = sign * g;
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) prior += __shfl_xor_sync(0xffffffffu, prior, off);
+  prior = tm.sum(prior);
   double lp = col(0) + prior;
   if (!propto) {
     if (m.link == LINK_NORMAL) lp += -(double)m.N * kLogSqrt2Pi;

@@ -35,6 +35,7 @@
 #include "loglik_finalize.cuh"
 #include "nuts_device.h"
 #include "tc_common.cuh"
+#include "team.cuh"
 
 namespace gbn {
 
@@ -42,12 +43,6 @@ namespace gbn {
 #define DADD(a, b) __dadd_rn((a), (b))
 #define DSUB(a, b) __dsub_rn((a), (b))
 #define DDIV(a, b) __ddiv_rn((a), (b))
-
-static __device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-  return v;
-}
 
 static __device__ __forceinline__ double log1p_exp_d(double a) {
   if (a > 0.0) return a + log1p(exp(-a));
@@ -66,15 +61,16 @@ static __device__ __forceinline__ double log_sum_exp_d(double a, double b) {
 struct Ctx {
   const SamplerCfg& cfg;
   double* vecs;
-  int c, lane;
+  int c, tid, nth;  // chain; thread index in the chain's team, team size
+  Team tm;
   __device__ double* slot(int s) const {
     return vecs + ((size_t)c * cfg.n_slots + s) * cfg.ld;
   }
 };
 
-// The chain's per-level stack in shared memory (one copy per warp).  All
-// lanes hold the same values; entries read and then rewritten by every lane
-// are separated by __syncwarp so no lane reads another lane's new value.
+// The chain's per-level stack in shared memory (one copy per team).  All
+// threads hold the same values; entries read and then rewritten by every
+// thread are separated by team barriers so none reads another's new value.
 struct Stk {
   double* lsw;
   double* V;
@@ -86,8 +82,8 @@ static __device__ double kinetic(const Ctx& x, const double* p) {
   const double* im = x.slot(SL_INVM);
   double s = 0.0;
 #pragma unroll 4
-  for (int i = x.lane; i < x.cfg.D; i += 32) s += p[i] * DMUL(im[i], p[i]);
-  return 0.5 * warp_sum(s);
+  for (int i = x.tid; i < x.cfg.D; i += x.nth) s += p[i] * DMUL(im[i], p[i]);
+  return 0.5 * x.tm.sum(s);
 }
 
 static __device__ __forceinline__ double draw_uniform(const SamplerCfg& cfg, ChainState& st,
@@ -99,7 +95,7 @@ static __device__ __forceinline__ double draw_uniform(const SamplerCfg& cfg, Cha
 static __device__ void sample_p(const Ctx& x, ChainState& st, double* p) {
   const double* im = x.slot(SL_INVM);
   const unsigned chain = x.cfg.init_chain_id + (unsigned)x.c;
-  for (int i = x.lane; i < x.cfg.D; i += 32)
+  for (int i = x.tid; i < x.cfg.D; i += x.nth)
     p[i] = DDIV(gbds_normal_at(x.cfg.seed, chain, st.nn + i), __dsqrt_rn(im[i]));
   st.nn += x.cfg.D;
 }
@@ -107,14 +103,14 @@ static __device__ void sample_p(const Ctx& x, ChainState& st, double* p) {
 static __device__ void copy_vec(const Ctx& x, double* __restrict__ dst,
                                 const double* __restrict__ src) {
 #pragma unroll 4
-  for (int i = x.lane; i < x.cfg.D; i += 32) dst[i] = src[i];
+  for (int i = x.tid; i < x.cfg.D; i += x.nth) dst[i] = src[i];
 }
 
 // begin_update_p / end_update_p: p -= (eps/2) g  (expl_leapfrog.hpp:16-28)
 static __device__ void half_kick(const Ctx& x, double* __restrict__ p,
                                  const double* __restrict__ g, double half) {
 #pragma unroll 4
-  for (int i = x.lane; i < x.cfg.D; i += 32) p[i] = DSUB(p[i], DMUL(half, g[i]));
+  for (int i = x.tid; i < x.cfg.D; i += x.nth) p[i] = DSUB(p[i], DMUL(half, g[i]));
 }
 
 // update_q: q += eps * invM p, then request the gradient at q.
@@ -123,7 +119,7 @@ static __device__ void drift_and_request(const Ctx& x, double* __restrict__ q,
                                          double* __restrict__ req) {
   const double* __restrict__ im = x.slot(SL_INVM);
 #pragma unroll 4
-  for (int i = x.lane; i < x.cfg.D; i += 32) {
+  for (int i = x.tid; i < x.cfg.D; i += x.nth) {
     double v = DADD(q[i], DMUL(eps, DMUL(im[i], p[i])));
     q[i] = v;
     req[i] = v;
@@ -133,8 +129,8 @@ static __device__ void drift_and_request(const Ctx& x, double* __restrict__ q,
 // The request as tensor-core coefficient words (features 0..127, zeros past
 // D), for the chains-on-M gradient kernel.  Reads back the warp's own writes.
 static __device__ void pack_request_words(const Ctx& x, const double* rq, uint32_t* w) {
-  __syncwarp();
-  for (int j = x.lane; j < tc::kThetaWords / 2; j += 32) {
+  x.tm.sync();
+  for (int j = x.tid; j < tc::kThetaWords / 2; j += x.nth) {
     const int k = 2 * j;
     uint32_t wh, wl;
     tc::theta_words(k < x.cfg.D ? rq[k] : 0.0, k + 1 < x.cfg.D ? rq[k + 1] : 0.0, wh, wl);
@@ -148,7 +144,7 @@ static __device__ void write_row(const Ctx& x, const ChainState& st, double* row
                                  double* diag) {
   const SamplerCfg& cfg = x.cfg;
   const double* q = x.slot(SL_SMP_Q);
-  if (x.lane == 0) {
+  if (x.tid == 0) {
     row[0] = -st.V_smp;
     row[1] = st.accept;
     row[2] = st.eps;
@@ -157,7 +153,7 @@ static __device__ void write_row(const Ctx& x, const ChainState& st, double* row
     row[5] = st.divergent;
     row[6] = st.energy;
   }
-  for (int i = x.lane; i < cfg.D; i += 32) {
+  for (int i = x.tid; i < cfg.D; i += x.nth) {
     double v = q[i];
     if (i == cfg.idx_tau || i == cfg.idx_sigma) v = exp(v);
     row[7 + i] = v;
@@ -165,7 +161,7 @@ static __device__ void write_row(const Ctx& x, const ChainState& st, double* row
   if (diag) {
     const double* p = x.slot(SL_SMP_P);
     const double* g = x.slot(SL_SMP_G);
-    for (int i = x.lane; i < cfg.D; i += 32) {
+    for (int i = x.tid; i < cfg.D; i += x.nth) {
       diag[i] = q[i];
       diag[cfg.D + i] = p[i];
       diag[2 * cfg.D + i] = g[i];
@@ -215,7 +211,7 @@ static __device__ int learn_variance(const Ctx& x, ChainState& st) {
   double* var = x.slot(SL_INVM);
   if (adaptation_window(st)) {
     st.w_n += 1.0;
-    for (int i = x.lane; i < D; i += 32) {
+    for (int i = x.tid; i < D; i += x.nth) {
       double delta = DSUB(q[i], m[i]);
       m[i] = DADD(m[i], DDIV(delta, st.w_n));
       m2[i] = DADD(m2[i], DMUL(DSUB(q[i], m[i]), delta));
@@ -227,7 +223,7 @@ static __device__ int learn_variance(const Ctx& x, ChainState& st) {
     const double a = n / (n + 5.0);
     const double b = 1e-3 * (5.0 / (n + 5.0));
     int bad = 0;
-    for (int i = x.lane; i < D; i += 32) {
+    for (int i = x.tid; i < D; i += x.nth) {
       double v = var[i];
       if (n > 1) v = DDIV(m2[i], n - 1.0);
       v = DADD(DMUL(a, v), b);
@@ -238,7 +234,7 @@ static __device__ int learn_variance(const Ctx& x, ChainState& st) {
     }
     st.w_n = 0.0;
     st.wa_counter += 1u;
-    bad = __any_sync(0xffffffffu, bad);
+    bad = x.tm.any(bad) ? 1 : 0;
     return bad ? -1 : 1;
   }
   st.wa_counter += 1u;
@@ -247,9 +243,9 @@ static __device__ int learn_variance(const Ctx& x, ChainState& st) {
 
 // The vector pass of an inner merge: rho and the edge momentum of level l,
 // its proposal if the final subtree is selected, and the six U-turn dot
-// products (partial per lane).  Pointers of the two subtrees never alias.
+// products (partial per thread).  Pointers of the two subtrees never alias.
 static __device__ __forceinline__ void merge_level_pass(
-    int D, int lane, double* __restrict__ IQ, double* __restrict__ IP, double* __restrict__ IG,
+    int D, int tid, int nth, double* __restrict__ IQ, double* __restrict__ IP, double* __restrict__ IG,
     const double* __restrict__ IPB, double* __restrict__ IPE, double* __restrict__ IR,
     const double* __restrict__ CQ, const double* __restrict__ CP, const double* __restrict__ CG,
     const double* __restrict__ CPB, const double* __restrict__ CPE,
@@ -257,7 +253,7 @@ static __device__ __forceinline__ void merge_level_pass(
     double* dd) {
   double d1a = 0, d1b = 0, d2a = 0, d2b = 0, d3a = 0, d3b = 0;
 #pragma unroll 2
-  for (int i = lane; i < D; i += 32) {
+  for (int i = tid; i < D; i += nth) {
     const double ipb = IPB[i], ipe = IPE[i], ir = IR[i];
     const double cpb = CPB[i], cpe = CPE[i], cr = CR[i];
     const double psb = DMUL(im[i], ipb);   // p_sharp_beg
@@ -290,9 +286,9 @@ static __device__ __forceinline__ void merge_level_pass(
 }
 
 // The vector pass of the top-level merge: trajectory rho and edge momenta,
-// the sample if selected, and the six U-turn dot products (partial per lane).
+// the sample if selected, and the six U-turn dot products (partial per thread).
 static __device__ __forceinline__ void merge_top_pass(
-    int D, int lane, bool fwd, bool sel, double* __restrict__ RHO, double* __restrict__ PFF,
+    int D, int tid, int nth, bool fwd, bool sel, double* __restrict__ RHO, double* __restrict__ PFF,
     double* __restrict__ PFB, double* __restrict__ PBF, double* __restrict__ PBB,
     double* __restrict__ SQ, double* __restrict__ SP, double* __restrict__ SG,
     const double* __restrict__ CQ, const double* __restrict__ CP, const double* __restrict__ CG,
@@ -300,7 +296,7 @@ static __device__ __forceinline__ void merge_top_pass(
     const double* __restrict__ CR, const double* __restrict__ im, double* dd) {
   double d1a = 0, d1b = 0, d2a = 0, d2b = 0, d3a = 0, d3b = 0;
 #pragma unroll 2
-  for (int i = lane; i < D; i += 32) {
+  for (int i = tid; i < D; i += nth) {
     double rho_bck, rho_fwd, p_ff, p_fb, p_bf, p_bb;
     if (fwd) {
       rho_bck = RHO[i];
@@ -390,19 +386,14 @@ static __device__ bool merge_into_level(const Ctx& x, ChainState& st, const Stk&
     sel_final = draw_uniform(cfg, st, x.c) < accept_prob;
   }
   double dd[6];
-  merge_level_pass(cfg.D, x.lane, IQ, IP, IG, IPB, IPE, IR, CQ, CP, CG, CPB, CPE, CR,
+  merge_level_pass(cfg.D, x.tid, x.nth, IQ, IP, IG, IPB, IPE, IR, CQ, CP, CG, CPB, CPE, CR,
                    x.slot(SL_INVM), sel_final, dd);
-  double d1a = dd[0], d1b = dd[1], d2a = dd[2], d2b = dd[3], d3a = dd[4], d3b = dd[5];
-  d1a = warp_sum(d1a);
-  d1b = warp_sum(d1b);
-  d2a = warp_sum(d2a);
-  d2b = warp_sum(d2b);
-  d3a = warp_sum(d3a);
-  d3b = warp_sum(d3b);
-  __syncwarp();
+  x.tm.sum6(dd);
+  const double d1a = dd[0], d1b = dd[1], d2a = dd[2], d2b = dd[3], d3a = dd[4], d3b = dd[5];
+  x.tm.sync();
   if (sel_final) sk.V[l] = cur_V;
   sk.lsw[l] = lsw_sub;
-  __syncwarp();
+  x.tm.sync();
   return (d1a > 0 && d1b > 0) && (d2a > 0 && d2b > 0) && (d3a > 0 && d3b > 0);
 }
 
@@ -447,32 +438,28 @@ static __device__ bool merge_top(const Ctx& x, ChainState& st, const Stk& sk, in
   const double* im = x.slot(SL_INVM);
   const bool fwd = st.dir > 0;
   double dd[6];
-  merge_top_pass(cfg.D, x.lane, fwd, sel, RHO, PFF, PFB, PBF, PBB, SQ, SP, SG, CQ, CP, CG, CPB,
+  merge_top_pass(cfg.D, x.tid, x.nth, fwd, sel, RHO, PFF, PFB, PBF, PBB, SQ, SP, SG, CQ, CP, CG, CPB,
                  CPE, CR, im, dd);
-  double d1a = dd[0], d1b = dd[1], d2a = dd[2], d2b = dd[3], d3a = dd[4], d3b = dd[5];
   if (sel) st.V_smp = cur_V;
-  d1a = warp_sum(d1a);
-  d1b = warp_sum(d1b);
-  d2a = warp_sum(d2a);
-  d2b = warp_sum(d2b);
-  d3a = warp_sum(d3a);
-  d3b = warp_sum(d3b);
+  x.tm.sum6(dd);
+  const double d1a = dd[0], d1b = dd[1], d2a = dd[2], d2b = dd[3], d3a = dd[4], d3b = dd[5];
   return (d1a > 0 && d1b > 0) && (d2a > 0 && d2b > 0) && (d3a > 0 && d3b > 0);
 }
 
-static __device__ void finish_chain(ChainState& st, int status, int* done_count, int lane) {
+static __device__ void finish_chain(ChainState& st, int status, int* done_count, int tid) {
   st.status = status;
   st.done = 1;
   st.phase = PH_DONE;
-  if (lane == 0) atomicAdd(done_count, 1);
+  if (tid == 0) atomicAdd(done_count, 1);
 }
 
 // One chain's step: runs its state machine from where it yielded to its next
 // gradient request (or to the end of its run).  Called by a whole warp.
 static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, const ModelDesc& m,
-                                                       const FitPtrs& f, int c, int lane,
+                                                       const FitPtrs& f, int c, const Team& tm,
                                                        double* lsw_s, double* V_s, int* slot_s,
                                                        double* cs_s) {
+  const int tid = tm.t, nth = tm.n;
   ChainState* __restrict__ states = f.states;
   ChainStack* __restrict__ stacks = f.stacks;
   double* vecs = f.vecs;
@@ -488,18 +475,18 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
   uint32_t* req_tc = f.req_tc ? f.req_tc + (size_t)c * tc::kThetaWords : nullptr;
   ChainState st = states[c];
   if (st.done) {
-    if (lane == 0) active[c] = 0;
+    if (tid == 0) active[c] = 0;
     return;
   }
-  if (lane < MAX_TREE_DEPTH) {
-    lsw_s[lane] = stacks[c].lsw[lane];
-    slot_s[lane] = stacks[c].slot[lane];
-  } else {
-    V_s[lane - MAX_TREE_DEPTH] = stacks[c].V[lane - MAX_TREE_DEPTH];
+  if (tid < MAX_TREE_DEPTH) {
+    lsw_s[tid] = stacks[c].lsw[tid];
+    slot_s[tid] = stacks[c].slot[tid];
+  } else if (tid < 2 * MAX_TREE_DEPTH) {
+    V_s[tid - MAX_TREE_DEPTH] = stacks[c].V[tid - MAX_TREE_DEPTH];
   }
-  __syncwarp();
+  tm.sync();
   const Stk sk{lsw_s, V_s, slot_s};
-  Ctx x{cfg, vecs, c, lane};
+  Ctx x{cfg, vecs, c, tid, nth, tm};
   const int D = cfg.D;
   double* rq = req + (size_t)c * cfg.ld;
   const double inf = __longlong_as_double(0x7ff0000000000000LL);
@@ -510,7 +497,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
   // partials into the working point's g slot (g = -grad lp); returns V.
   auto resume = [&](int q_slot, int g_slot) -> double {
     const double lp = finalize_chain(m, x.slot(q_slot), c, cfg.C, pv.P, pv.NP, pv.S, pv.Gz,
-                                     x.slot(g_slot), -1.0, 1, 1, lane, cs_s);
+                                     x.slot(g_slot), -1.0, 1, 1, tm, cs_s);
     if (isnan(lp)) return lp;
     if (!isfinite(lp)) return inf;
     return -lp;
@@ -518,14 +505,14 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
 
   while (!yield && !st.done) {
     if (++guard > 64) {
-      finish_chain(st, GBNUTS_CHAIN_STEPSIZE_FAILED, done_count, lane);
+      finish_chain(st, GBNUTS_CHAIN_STEPSIZE_FAILED, done_count, tid);
       break;
     }
     switch (st.phase) {
       case PH_INIT_DRAW: {
         // initialize.hpp:68-227: user values, zeros, or uniform(-R, R)
         double* q = x.slot(SL_FWD_Q);
-        for (int i = lane; i < D; i += 32) {
+        for (int i = tid; i < D; i += nth) {
           double v;
           if (inits)
             v = inits[(size_t)c * D + i];
@@ -550,8 +537,8 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         const double V0 = resume(SL_FWD_Q, SL_FWD_G);
         double gs = 0.0;
         const double* g0 = x.slot(SL_FWD_G);
-        for (int i = lane; i < D; i += 32) gs += g0[i];
-        gs = warp_sum(gs);
+        for (int i = tid; i < D; i += nth) gs += g0[i];
+        gs = tm.sum(gs);
         if (isfinite(V0) && isfinite(gs)) {
           copy_vec(x, x.slot(SL_SMP_Q), x.slot(SL_FWD_Q));
           copy_vec(x, x.slot(SL_SMP_G), x.slot(SL_FWD_G));
@@ -567,7 +554,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
           st.init_try += 1;
           const int max_tries = (inits || cfg.init_radius == 0.0) ? 1 : 100;
           if (st.init_try >= max_tries)
-            finish_chain(st, GBNUTS_CHAIN_INIT_FAILED, done_count, lane);
+            finish_chain(st, GBNUTS_CHAIN_INIT_FAILED, done_count, tid);
           else
             st.phase = PH_INIT_DRAW;
         }
@@ -592,7 +579,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         copy_vec(x, g, x.slot(SL_SMP_G));
         st.V_fwd = st.V_smp;
         sample_p(x, st, p);
-        __syncwarp();
+        tm.sync();
         st.ss_H0 = kinetic(x, p) + st.V_fwd;
         const double e = st.nom_eps;
         half_kick(x, p, g, 0.5 * e);
@@ -608,7 +595,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         double* g = x.slot(SL_FWD_G);
         st.V_fwd = resume(SL_FWD_Q, SL_FWD_G);
         half_kick(x, p, g, 0.5 * st.nom_eps);
-        __syncwarp();
+        tm.sync();
         double h = kinetic(x, p) + st.V_fwd;
         if (isnan(h)) h = inf;
         const double dH = st.ss_H0 - h;
@@ -631,7 +618,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
           finish_chain(st,
                        st.ss_ctx == SS_CTX_START ? GBNUTS_CHAIN_STEPSIZE_INIT_FAILED
                                                  : GBNUTS_CHAIN_STEPSIZE_FAILED,
-                       done_count, lane);
+                       done_count, tid);
           st.ss_fail = st.nom_eps > 1e7 ? 1 : 2;
           break;
         }
@@ -659,11 +646,11 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
           st.warm_end_ngrad = st.n_grad;
         }
         if (st.iter >= cfg.num_warmup + cfg.num_samples) {
-          finish_chain(st, GBNUTS_CHAIN_OK, done_count, lane);
+          finish_chain(st, GBNUTS_CHAIN_OK, done_count, tid);
           break;
         }
         if (abort_flag && *abort_flag) {
-          finish_chain(st, GBNUTS_CHAIN_INTERRUPTED, done_count, lane);
+          finish_chain(st, GBNUTS_CHAIN_INTERRUPTED, done_count, tid);
           break;
         }
         st.phase = PH_TRANS_BEGIN;
@@ -677,7 +664,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
                         DADD(1.0, DMUL(cfg.jitter, DSUB(2.0 * draw_uniform(cfg, st, c), 1.0))));
         double* SP = x.slot(SL_SMP_P);
         sample_p(x, st, SP);
-        __syncwarp();
+        tm.sync();
         const double* SQ = x.slot(SL_SMP_Q);
         const double* SG = x.slot(SL_SMP_G);
         double* FQ = x.slot(SL_FWD_Q);
@@ -691,7 +678,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         double* PBF = x.slot(SL_PBF);
         double* PBB = x.slot(SL_PBB);
         double* RHO = x.slot(SL_RHO);
-        for (int i = lane; i < D; i += 32) {
+        for (int i = tid; i < D; i += nth) {
           const double q = SQ[i], p = SP[i], g = SG[i];
           FQ[i] = q;
           FP[i] = p;
@@ -724,9 +711,9 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         st.dir = draw_uniform(cfg, st, c) > 0.5 ? 1 : -1;
         st.sub_d = st.depth;
         st.leaf = 0;
-        __syncwarp();
-        if (lane < MAX_TREE_DEPTH) sk.slot[lane] = lane;
-        __syncwarp();
+        tm.sync();
+        if (tid < MAX_TREE_DEPTH) sk.slot[tid] = tid;
+        tm.sync();
         st.phase = PH_LEAF_BEGIN;
         break;
       }
@@ -758,7 +745,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
           st.V_bck = V;
         const double e = st.dir * st.eps;
         half_kick(x, p, g, 0.5 * e);
-        __syncwarp();
+        tm.sync();
         // leaf of build_tree (base_nuts.hpp:253-281)
         st.n_lf += 1;
         double h = kinetic(x, p) + V;
@@ -781,7 +768,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         double cur_V = V;
         bool ok = true;
         while (l < d && ((i >> l) & 1)) {
-          __syncwarp();
+          tm.sync();
           ok = merge_into_level(x, st, sk, l, cur_level, wq, wp, wg, cur_lsw, cur_V);
           cur_level = l;
           cur_lsw = sk.lsw[l];
@@ -804,7 +791,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
             double* IPE = x.slot(base_i + 4);
             double* IR = x.slot(base_i + 5);
             const double* Q = x.slot(wq);
-            for (int k = lane; k < D; k += 32) {
+            for (int k = tid; k < D; k += nth) {
               const double pk = p[k];
               IQ[k] = Q[k];
               IP[k] = pk;
@@ -813,26 +800,26 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
               IPE[k] = pk;
               IR[k] = pk;
             }
-            __syncwarp();
+            tm.sync();
             sk.lsw[0] = w;
             sk.V[0] = V;
-            __syncwarp();
+            tm.sync();
           } else {
             // the merged subtree at level l-1 becomes the left sibling at level l
             const int sa = sk.slot[l], sb = sk.slot[l - 1];
             const double la = sk.lsw[l - 1], va = sk.V[l - 1];
-            __syncwarp();
+            tm.sync();
             sk.slot[l] = sb;
             sk.slot[l - 1] = sa;
             sk.lsw[l] = la;
             sk.V[l] = va;
-            __syncwarp();
+            tm.sync();
           }
           st.leaf += 1;
           st.phase = PH_LEAF_BEGIN;
           break;
         }
-        __syncwarp();
+        tm.sync();
         const bool persist = merge_top(x, st, sk, cur_level, wq, wp, wg, cur_lsw, cur_V);
         st.phase = persist ? PH_DOUBLING : PH_TRANS_END;
         break;
@@ -840,7 +827,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
       case PH_TRANS_END: {
         // base_nuts.hpp:195-203, then generate_transitions' write and
         // adapt_diag_e_nuts' learning
-        __syncwarp();
+        tm.sync();
         st.accept = st.sum_metro / (double)st.n_lf;
         st.energy = kinetic(x, x.slot(SL_SMP_P)) + st.V_smp;
         const int m = st.iter;
@@ -860,10 +847,10 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         st.phase = PH_AFTER_ITER;
         if (st.adapt_flag) {
           learn_stepsize(cfg, st, st.accept);
-          __syncwarp();
+          tm.sync();
           const int upd = learn_variance(x, st);
           if (upd < 0) {
-            finish_chain(st, GBNUTS_CHAIN_METRIC_OVERFLOW, done_count, lane);
+            finish_chain(st, GBNUTS_CHAIN_METRIC_OVERFLOW, done_count, tid);
             break;
           }
           if (upd > 0) {
@@ -874,48 +861,55 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         break;
       }
       default:
-        finish_chain(st, GBNUTS_CHAIN_STEPSIZE_FAILED, done_count, lane);
+        finish_chain(st, GBNUTS_CHAIN_STEPSIZE_FAILED, done_count, tid);
         break;
     }
-    __syncwarp();
+    tm.sync();
   }
-  __syncwarp();
-  if (lane < MAX_TREE_DEPTH) {
-    stacks[c].lsw[lane] = sk.lsw[lane];
-    stacks[c].slot[lane] = sk.slot[lane];
-  } else {
-    stacks[c].V[lane - MAX_TREE_DEPTH] = sk.V[lane - MAX_TREE_DEPTH];
+  tm.sync();
+  if (tid < MAX_TREE_DEPTH) {
+    stacks[c].lsw[tid] = sk.lsw[tid];
+    stacks[c].slot[tid] = sk.slot[tid];
+  } else if (tid < 2 * MAX_TREE_DEPTH) {
+    stacks[c].V[tid - MAX_TREE_DEPTH] = sk.V[tid - MAX_TREE_DEPTH];
   }
-  if (lane == 0) {
+  if (tid == 0) {
     states[c] = st;
     active[c] = (yield && !st.done) ? 1 : 0;
   }
 }
 
-// Chains of one or many fits in one launch: warp g runs chain chain_map[g].y
-// of fit chain_map[g].x.  A single-fit run launches the same kernel with a
-// one-entry table, so a fit's arithmetic is the same compiled code alone and
-// in a pool.  Each warp first copies its fit's descriptor to shared memory.
-__global__ void __launch_bounds__(128, 1)
+// Chains of one or many fits in one launch: team g runs chain chain_map[g].y
+// of fit chain_map[g].x.  W = 1: one warp per chain, four chains per CTA;
+// W > 1: one chain per CTA of W warps (large dimensions).  A single-fit run
+// launches the same kernel with a one-entry table, so a fit's arithmetic is
+// the same compiled code alone and in a pool.  Each team first copies its
+// fit's descriptor to shared memory.
+template <int W>
+__global__ void __launch_bounds__(W == 1 ? 128 : 32 * W, 1)
     nuts_step_pool_kernel(const PoolFitDev* __restrict__ fits, const int2* __restrict__ chain_map,
                           int total) {
-  __shared__ double sh_lsw[4][MAX_TREE_DEPTH];
-  __shared__ double sh_V[4][MAX_TREE_DEPTH];
-  __shared__ int sh_slot[4][MAX_TREE_DEPTH];
-  __shared__ double sh_cs[4][kMaxColSums];
-  __shared__ PoolFitDev sh_fit[4];
+  constexpr int CPB = (W == 1) ? 4 : 1;  // chains per CTA
+  __shared__ double sh_lsw[CPB][MAX_TREE_DEPTH];
+  __shared__ double sh_V[CPB][MAX_TREE_DEPTH];
+  __shared__ int sh_slot[CPB][MAX_TREE_DEPTH];
+  __shared__ double sh_cs[CPB][kMaxColSums];
+  __shared__ PoolFitDev sh_fit[CPB];
+  __shared__ double sh_red[8 * W];
   static_assert(sizeof(PoolFitDev) % 8 == 0, "descriptor copied as 8-byte words");
-  const int g = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  const int wl = threadIdx.x >> 5;
-  if (g >= total) return;  // uniform per warp
+  const int g = (W == 1) ? (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5)
+                         : (int)blockIdx.x;
+  const int t = (W == 1) ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
+  const int k = (W == 1) ? (int)(threadIdx.x >> 5) : 0;
+  if (g >= total) return;  // uniform per team
+  const Team tm{t, 32 * W, W, sh_red};
   const int2 fc = chain_map[g];
   const unsigned long long* src = reinterpret_cast<const unsigned long long*>(fits + fc.x);
-  unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sh_fit[wl]);
-  for (int i = lane; i < (int)(sizeof(PoolFitDev) / 8); i += 32) dst[i] = src[i];
-  __syncwarp();
-  const PoolFitDev& pf = sh_fit[wl];
-  nuts_step_chain(pf.cfg, pf.m, pf.f, fc.y, lane, sh_lsw[wl], sh_V[wl], sh_slot[wl], sh_cs[wl]);
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sh_fit[k]);
+  for (int i = t; i < (int)(sizeof(PoolFitDev) / 8); i += 32 * W) dst[i] = src[i];
+  tm.sync();
+  const PoolFitDev& pf = sh_fit[k];
+  nuts_step_chain(pf.cfg, pf.m, pf.f, fc.y, tm, sh_lsw[k], sh_V[k], sh_slot[k], sh_cs[k]);
 }
 
 // Sets every chain's state from the configuration (service set-up,
@@ -965,12 +959,18 @@ void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* sta
   nuts_init_kernel<<<blocks, threads, 0, s>>>(cfg, states, stacks, vecs, inv_metrics, active);
 }
 
-void launch_nuts_step_pool(const PoolFitDev* fits, const int2* chain_map, int total,
+void launch_nuts_step_pool(const PoolFitDev* fits, const int2* chain_map, int total, int team,
                            cudaStream_t s) {
   if (total <= 0) return;
-  const int threads = 128;
-  const int blocks = (int)(((size_t)total * 32 + threads - 1) / threads);
-  nuts_step_pool_kernel<<<blocks, threads, 0, s>>>(fits, chain_map, total);
+  if (team == 1) {
+    const int threads = 128;
+    const int blocks = (int)(((size_t)total * 32 + threads - 1) / threads);
+    nuts_step_pool_kernel<1><<<blocks, threads, 0, s>>>(fits, chain_map, total);
+  } else if (team == 2) {
+    nuts_step_pool_kernel<2><<<total, 64, 0, s>>>(fits, chain_map, total);
+  } else {
+    nuts_step_pool_kernel<4><<<total, 128, 0, s>>>(fits, chain_map, total);
+  }
 }
 
 }  // namespace gbn

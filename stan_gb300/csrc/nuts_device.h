@@ -106,8 +106,12 @@ struct PoolFitDev {
   FitPtrs f;
 };
 
-// One step of `total` chains: chain_map[g] = (table index, chain in fit).
-void launch_nuts_step_pool(const PoolFitDev* fits, const int2* chain_map, int total,
+// Warps per chain of the step kernel for a dimension D (1, 2 or 4).
+inline int team_warps(int D) { return D <= 256 ? 1 : (D <= 1024 ? 2 : 4); }
+
+// One step of `total` chains: chain_map[g] = (table index, chain in fit); all
+// of them with `team` warps per chain (team_warps of their fit's D).
+void launch_nuts_step_pool(const PoolFitDev* fits, const int2* chain_map, int total, int team,
                            cudaStream_t s);
 
 }  // namespace gbn

@@ -120,6 +120,7 @@ struct gbnuts_pool {
   PoolWorkItem* d_items = nullptr;
   size_t cap_fits = 0, cap_gfits = 0, cap_chains = 0, cap_items = 0;
   int n_chain_map = 0, n_items = 0;
+  int team_off[3] = {0, 0, 0}, team_n[3] = {0, 0, 0};  // chain map by team size
   size_t smem = 0;
 };
 
@@ -286,7 +287,7 @@ static cudaError_t grow(T** buf, size_t* cap, size_t need) {
 static int rebuild_tables(gbnuts_pool* p) {
   std::vector<PoolFitDev> fits;
   std::vector<PoolGradFit> gfits;
-  std::vector<int2> cmap;
+  std::vector<int2> cmap_team[3];  // chains by team size 1, 2, 4 warps
   std::vector<PoolWorkItem> items;
   size_t smem = 0;
   for (size_t i = 0; i < p->active.size(); ++i) {
@@ -310,11 +311,19 @@ static int rebuild_tables(gbnuts_pool* p) {
     g.NP = f->NP;
     g.Gz = f->Gz;
     gfits.push_back(g);
-    for (int c = 0; c < f->C; ++c) cmap.push_back(make_int2((int)i, c));
+    const int tw = team_warps(f->cfg.D);
+    for (int c = 0; c < f->C; ++c)
+      cmap_team[tw == 1 ? 0 : (tw == 2 ? 1 : 2)].push_back(make_int2((int)i, c));
     const int blocks = (f->C + 15) / 16;
     for (int s = 0; s < f->S; ++s)
       for (int b = 0; b < blocks; ++b) items.push_back(PoolWorkItem{(int)i, s, b, f->rb});
     smem = std::max(smem, f->smem);
+  }
+  std::vector<int2> cmap;
+  for (int k = 0; k < 3; ++k) {
+    p->team_off[k] = (int)cmap.size();
+    p->team_n[k] = (int)cmap_team[k].size();
+    cmap.insert(cmap.end(), cmap_team[k].begin(), cmap_team[k].end());
   }
   cudaError_t e = grow(&p->d_fits, &p->cap_fits, fits.size());
   if (e == cudaSuccess) e = grow(&p->d_gfits, &p->cap_gfits, gfits.size());
@@ -451,7 +460,9 @@ int gbnuts_pool_step(gbnuts_pool* p, int n_steps, int* n_running, int* n_queued)
   }
   if (!p->active.empty() && n_steps > 0) {
     for (int k = 0; k < n_steps; ++k) {
-      launch_nuts_step_pool(p->d_fits, p->d_chain_map, p->n_chain_map, p->stream);
+      for (int k = 0; k < 3; ++k)
+        launch_nuts_step_pool(p->d_fits, p->d_chain_map + p->team_off[k], p->team_n[k], 1 << k,
+                              p->stream);
       for (ActiveFit* f : p->active)
         if (f->memset_gz)
           cudaMemsetAsync(f->Gz, 0, (size_t)f->C * f->model->desc.J * 8, p->stream);

@@ -90,3 +90,21 @@ def test_draw_stream_matches_host():
     for c in range(3):
         u = oracle.draws(1234, 7 + c, 0, 0, m.D)
         assert np.array_equal(r.init[c], (2.0 * u - 1.0) * 1.5)
+
+
+@pytest.mark.parametrize("J", [300, 1100])
+def test_multi_warp_chains_replay(J):
+    """Large dimensions run one chain per CTA of 2 (D <= 1024) or 4 warps;
+    their transitions replay the oracle like the warp-per-chain form."""
+    from stan_gb300 import Model, sampler, workloads
+    ds = workloads.hier_normal(J=J, K=6, mean_size=4, seed=11)
+    m = Model.from_dataset(ds)
+    om = ds.oracle_model()
+    C = 3
+    inits = np.random.default_rng(2).normal(size=(C, m.D)) * 0.1
+    kw = dict(num_chains=C, adapt=False, num_warmup=0, num_samples=4, stepsize=0.05,
+              inits=inits, max_depth=6)
+    r = sampler.run(m, random_seed=9, **kw)
+    o = om.sample(seed=9, **kw)
+    assert np.all(r.status == 0) and np.all(o["return_code"] == 0)
+    _compare(r, o, 4)

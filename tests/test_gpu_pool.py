@@ -8,6 +8,7 @@ must be bit-identical.
 import numpy as np
 import pytest
 
+from stan_gb300 import workloads
 from tests.datasets import make_dataset
 
 pytestmark = pytest.mark.gpu
@@ -25,6 +26,8 @@ def _fits():
         (make_dataset("hier_logistic", small=True, seed=4), dict(base, num_chains=3, random_seed=13)),
         (make_dataset("poisson", small=True, seed=5),
          dict(base, num_chains=5, random_seed=14, num_warmup=80, save_warmup=True)),
+        (workloads.hier_logistic(15000, 8, seed=7),  # D = 310: two warps per chain
+         dict(base, num_chains=2, random_seed=16, num_warmup=60, num_samples=40)),
         (make_dataset("logistic_100k", small=True, seed=6),
          dict(num_chains=2, random_seed=15, adapt=False, num_warmup=0, num_samples=60,
               stepsize=0.2, max_depth=6)),
