@@ -251,7 +251,7 @@ int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* cfg,
  * (hmc_nuts_diag_e_adapt.hpp:331-407); a pool runs each submitted fit as
  * gbnuts_sample_run would (same draws, same chain status) while every
  * admitted fit shares the step launches.  Forms: GBNUTS_PREC_FP64 / FP32;
- * every fit in a pool stores X as the pool's x_dtype and has K <= 512. */
+ * every fit in a pool stores X as the pool's x_dtype and has K <= 2048. */
 typedef struct gbnuts_pool gbnuts_pool;
 
 /* max_fits: fits admitted at once; max_chains: chains admitted at once;

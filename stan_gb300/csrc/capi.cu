@@ -610,7 +610,8 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   GBN_CUDA_TRY(dr.alloc(&d_cmap, C));
   GBN_CUDA_TRY(cudaMemcpyAsync(d_fit, &h_fit, sizeof(h_fit), cudaMemcpyHostToDevice, st));
   GBN_CUDA_TRY(cudaMemcpyAsync(d_cmap, h_cmap.data(), C * sizeof(int2), cudaMemcpyHostToDevice, st));
-  const bool pool_partials = !is_tensor_precision(rc->precision) && chains_per_block(m->desc.K) == 16;
+  const bool pool_partials = !is_tensor_precision(rc->precision);
+  const int blk_chains = block_chains(m->desc.K, C);
   PoolGradFit* d_gfit = nullptr;
   PoolWorkItem* d_items = nullptr;
   int n_items = 0;
@@ -618,11 +619,12 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   if (pool_partials) {
     const PoolGradFit g{m->desc, d_req, cfg.ld, C, d_active, m->ws.split_rows, m->ws.partial,
                         m->ws.NP, m->ws.gz};
-    const int rb = partial_tile_rows(m->desc.K, rc->precision);
-    pool_smem = partial_smem(m->desc.K, rb, rc->precision);
+    const int rb = partial_tile_rows(m->desc.K, C, rc->precision);
+    pool_smem = partial_smem(m->desc.K, C, rb, rc->precision);
     std::vector<PoolWorkItem> items;
     for (int s = 0; s < m->ws.S; ++s)
-      for (int b = 0; b < (C + 15) / 16; ++b) items.push_back(PoolWorkItem{0, s, b, rb});
+      for (int b = 0; b < (C + blk_chains - 1) / blk_chains; ++b)
+        items.push_back(PoolWorkItem{0, s, b, rb});
     n_items = (int)items.size();
     GBN_CUDA_TRY(dr.alloc(&d_gfit, 1));
     GBN_CUDA_TRY(dr.alloc(&d_items, items.size()));
@@ -643,7 +645,7 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
     if (m->desc.off_z >= 0)
       GBN_CUDA_TRY(cudaMemsetAsync(m->ws.gz, 0, (size_t)C * m->desc.J * sizeof(double), st));
     if (e0) cudaEventRecord(e0, st);
-    int r = launch_partials_pool(d_gfit, d_items, n_items, m->desc.x_dtype, rc->precision,
+    int r = launch_partials_pool(d_gfit, d_items, n_items, blk_chains, m->desc.x_dtype, rc->precision,
                                  pool_smem, st);
     if (e1) cudaEventRecord(e1, st);
     return r;

@@ -113,16 +113,19 @@ struct PoolWorkItem {
 };
 // Tile rows the partial kernel uses for a given K (same choice as a
 // single-fit launch, so a fit's sums do not depend on its pool neighbours).
-int partial_tile_rows(int K, int precision);
-size_t partial_smem(int K, int rb, int precision);
-// Launches the pool partial kernel for work items whose fits share x_dtype;
-// every fit must have chains_per_block(K) == 16.
+int partial_tile_rows(int K, int C, int precision);
+size_t partial_smem(int K, int C, int rb, int precision);
+// Launches the pool partial kernel for work items whose fits share x_dtype
+// and block_chains (cb: 4, 8 or 16).
 int launch_partials_pool(const PoolGradFit* d_fits, const PoolWorkItem* d_items, int n_items,
-                         int x_dtype, int precision, size_t smem, cudaStream_t st);
+                         int cb, int x_dtype, int precision, size_t smem, cudaStream_t st);
 
 // Maximum chains per block of the partial kernel for a given K (0 if K is
 // beyond what the kernel supports).
 int chains_per_block(int K);
+// Chains per block a fit of C chains uses (the smaller of chains_per_block(K)
+// and C rounded up to 4, 8 or 16): fewer idle threads for small fits.
+int block_chains(int K, int C);
 
 // Tensor-core (bf16 hi/lo) GLM path.
 int tc_max_features();

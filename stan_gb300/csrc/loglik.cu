@@ -41,6 +41,11 @@ int chains_per_block(int K) {
   return 0;
 }
 
+int block_chains(int K, int C) {
+  const int by_c = C <= 4 ? 4 : (C <= 8 ? 8 : 16);
+  return std::min(chains_per_block(K), by_c);
+}
+
 template <typename XT>
 __device__ __forceinline__ double x_to_double(XT v);
 template <>
@@ -360,7 +365,7 @@ static void launch_partial(const ModelDesc& m, const double* Q, int ldq, int C,
 template <typename XT, typename CT>
 static void dispatch_cb(const ModelDesc& m, const double* Q, int ldq, int C,
                         const int* active, GradWorkspace& ws, cudaStream_t st) {
-  switch (chains_per_block(m.K)) {
+  switch (block_chains(m.K, C)) {
     case 16: launch_partial<XT, CT, 16>(m, Q, ldq, C, active, ws, st); break;
     case 8: launch_partial<XT, CT, 8>(m, Q, ldq, C, active, ws, st); break;
     default: launch_partial<XT, CT, 4>(m, Q, ldq, C, active, ws, st); break;
@@ -378,46 +383,54 @@ static void dispatch_x(const ModelDesc& m, const double* Q, int ldq, int C,
     dispatch_cb<uint16_t, CT>(m, Q, ldq, C, active, ws, st);
 }
 
-int partial_tile_rows(int K, int precision) {
-  const int CB = chains_per_block(K);
+int partial_tile_rows(int K, int C, int precision) {
+  const int CB = block_chains(K, C);
   return precision == GBNUTS_PREC_FP64 ? choose_rb<double>(CB, K) : choose_rb<float>(CB, K);
 }
 
-size_t partial_smem(int K, int rb, int precision) {
-  const int CB = chains_per_block(K);
+size_t partial_smem(int K, int C, int rb, int precision) {
+  const int CB = block_chains(K, C);
   return precision == GBNUTS_PREC_FP64 ? partial_smem_bytes<double>(CB, K, rb)
                                        : partial_smem_bytes<float>(CB, K, rb);
 }
 
-template <typename XT, typename CT>
+template <typename XT, typename CT, int CB>
 static int launch_pool_t(const PoolGradFit* d_fits, const PoolWorkItem* d_items, int n_items,
                          size_t smem, cudaStream_t st) {
   static size_t done = 0;
   {
     std::lock_guard<std::mutex> lk(g_attr_mu);
     if (smem > done) {
-      GBN_CUDA_TRY(cudaFuncSetAttribute(loglik_partial_pool_kernel<XT, CT, 16>,
+      GBN_CUDA_TRY(cudaFuncSetAttribute(loglik_partial_pool_kernel<XT, CT, CB>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       done = smem;
     }
   }
-  loglik_partial_pool_kernel<XT, CT, 16><<<n_items, kThreads, smem, st>>>(d_fits, d_items);
+  loglik_partial_pool_kernel<XT, CT, CB><<<n_items, kThreads, smem, st>>>(d_fits, d_items);
   GBN_CUDA_TRY(cudaGetLastError());
   return GBNUTS_OK;
 }
 
+template <typename XT, typename CT>
+static int launch_pool_cb(const PoolGradFit* d_fits, const PoolWorkItem* d_items, int n_items,
+                          int cb, size_t smem, cudaStream_t st) {
+  if (cb == 4) return launch_pool_t<XT, CT, 4>(d_fits, d_items, n_items, smem, st);
+  if (cb == 8) return launch_pool_t<XT, CT, 8>(d_fits, d_items, n_items, smem, st);
+  return launch_pool_t<XT, CT, 16>(d_fits, d_items, n_items, smem, st);
+}
+
 int launch_partials_pool(const PoolGradFit* d_fits, const PoolWorkItem* d_items, int n_items,
-                         int x_dtype, int precision, size_t smem, cudaStream_t st) {
+                         int cb, int x_dtype, int precision, size_t smem, cudaStream_t st) {
   if (n_items <= 0) return GBNUTS_OK;
   const bool f64 = precision == GBNUTS_PREC_FP64;
   if (x_dtype == GBNUTS_F64)
-    return f64 ? launch_pool_t<double, double>(d_fits, d_items, n_items, smem, st)
-               : launch_pool_t<double, float>(d_fits, d_items, n_items, smem, st);
+    return f64 ? launch_pool_cb<double, double>(d_fits, d_items, n_items, cb, smem, st)
+               : launch_pool_cb<double, float>(d_fits, d_items, n_items, cb, smem, st);
   if (x_dtype == GBNUTS_F32)
-    return f64 ? launch_pool_t<float, double>(d_fits, d_items, n_items, smem, st)
-               : launch_pool_t<float, float>(d_fits, d_items, n_items, smem, st);
-  return f64 ? launch_pool_t<uint16_t, double>(d_fits, d_items, n_items, smem, st)
-             : launch_pool_t<uint16_t, float>(d_fits, d_items, n_items, smem, st);
+    return f64 ? launch_pool_cb<float, double>(d_fits, d_items, n_items, cb, smem, st)
+               : launch_pool_cb<float, float>(d_fits, d_items, n_items, cb, smem, st);
+  return f64 ? launch_pool_cb<uint16_t, double>(d_fits, d_items, n_items, cb, smem, st)
+             : launch_pool_cb<uint16_t, float>(d_fits, d_items, n_items, cb, smem, st);
 }
 
 bool tc_chains_on_m() {
@@ -443,7 +456,7 @@ int choose_splits(const ModelDesc& m, int C, int precision) {
     if (!tc_supported(m)) return 1;  // wide-design GEMM form: one partial row per chain
     return tc_chains_on_m() ? tct_splits(m, C) : tc_splits(m, C);
   }
-  const int CB = chains_per_block(m.K);
+  const int CB = block_chains(m.K, C);
   const int chain_blocks = (C + CB - 1) / CB;
   // Splits: enough CTAs for ~2 waves over 152 SMs, a minimum of rows each.
   long long max_s = std::max(1LL, m.N / split_rows_min());

@@ -101,11 +101,7 @@ extern "C" int gbnuts_log_prob_grad_batch_device_noalloc(gbnuts_model* m, int C,
     return GBNUTS_USAGE;
   }
   // Row splits exactly as the regular entry point chooses them.
-  const int chain_blocks = (C + CB - 1) / CB;
-  long long max_s = std::max(1LL, desc.N / 64);
-  int S = (int)std::min<long long>(max_s, std::max(1, (2 * 152 + chain_blocks - 1) / chain_blocks));
-  if (desc.off_z >= 0) S = std::min(S, desc.J);
-  S = std::max(S, 1);
+  int S = choose_splits(desc, C, precision);
   constexpr int kMaxSplits = 512;
   if (S > kMaxSplits) S = kMaxSplits;
   const int NP = n_partials(desc);

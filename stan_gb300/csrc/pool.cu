@@ -61,7 +61,7 @@ struct ActiveFit {
   double* P = nullptr;
   double* Gz = nullptr;
   long long* split_rows = nullptr;
-  int S = 0, NP = 0, rb = 0;
+  int S = 0, NP = 0, rb = 0, cb = 16;
   size_t smem = 0;
   bool memset_gz = false;
   gbnuts_run_output* out = nullptr;
@@ -121,7 +121,8 @@ struct gbnuts_pool {
   size_t cap_fits = 0, cap_gfits = 0, cap_chains = 0, cap_items = 0;
   int n_chain_map = 0, n_items = 0;
   int team_off[3] = {0, 0, 0}, team_n[3] = {0, 0, 0};  // chain map by team size
-  size_t smem = 0;
+  int item_off[3] = {0, 0, 0}, item_n[3] = {0, 0, 0};  // work items by chains per block
+  size_t smem_cb[3] = {0, 0, 0};
 };
 
 enum { POOL_QUEUED = 0, POOL_RUNNING = 1, POOL_DONE = 2, POOL_UNKNOWN = 3 };
@@ -155,8 +156,9 @@ static int admit(gbnuts_pool* p, PendingFit& pf, bool force) {
   f->C = C;
   f->S = choose_splits(d, C, p->precision);
   f->NP = n_partials(d);
-  f->rb = partial_tile_rows(d.K, p->precision);
-  f->smem = partial_smem(d.K, f->rb, p->precision);
+  f->cb = block_chains(d.K, C);
+  f->rb = partial_tile_rows(d.K, C, p->precision);
+  f->smem = partial_smem(d.K, C, f->rb, p->precision);
   const int J = d.off_z >= 0 ? d.J : 0;
   const size_t need = fit_state_bytes(f->cfg, f->S, f->NP, J, pf.out->max_rows,
                                       pf.out->diagnostics != nullptr);
@@ -288,8 +290,8 @@ static int rebuild_tables(gbnuts_pool* p) {
   std::vector<PoolFitDev> fits;
   std::vector<PoolGradFit> gfits;
   std::vector<int2> cmap_team[3];  // chains by team size 1, 2, 4 warps
-  std::vector<PoolWorkItem> items;
-  size_t smem = 0;
+  std::vector<PoolWorkItem> items_cb[3];  // work items by chains per block 4, 8, 16
+  size_t smem_cb[3] = {0, 0, 0};
   for (size_t i = 0; i < p->active.size(); ++i) {
     ActiveFit* f = p->active[i];
     PoolFitDev pf;
@@ -314,10 +316,18 @@ static int rebuild_tables(gbnuts_pool* p) {
     const int tw = team_warps(f->cfg.D);
     for (int c = 0; c < f->C; ++c)
       cmap_team[tw == 1 ? 0 : (tw == 2 ? 1 : 2)].push_back(make_int2((int)i, c));
-    const int blocks = (f->C + 15) / 16;
+    const int kc = f->cb == 4 ? 0 : (f->cb == 8 ? 1 : 2);
+    const int blocks = (f->C + f->cb - 1) / f->cb;
     for (int s = 0; s < f->S; ++s)
-      for (int b = 0; b < blocks; ++b) items.push_back(PoolWorkItem{(int)i, s, b, f->rb});
-    smem = std::max(smem, f->smem);
+      for (int b = 0; b < blocks; ++b) items_cb[kc].push_back(PoolWorkItem{(int)i, s, b, f->rb});
+    smem_cb[kc] = std::max(smem_cb[kc], f->smem);
+  }
+  std::vector<PoolWorkItem> items;
+  for (int k = 0; k < 3; ++k) {
+    p->item_off[k] = (int)items.size();
+    p->item_n[k] = (int)items_cb[k].size();
+    p->smem_cb[k] = smem_cb[k];
+    items.insert(items.end(), items_cb[k].begin(), items_cb[k].end());
   }
   std::vector<int2> cmap;
   for (int k = 0; k < 3; ++k) {
@@ -346,7 +356,6 @@ static int rebuild_tables(gbnuts_pool* p) {
   if (e != cudaSuccess) return fail(GBNUTS_SOFTWARE, std::string("pool tables: ") + cudaGetErrorString(e));
   p->n_chain_map = (int)cmap.size();
   p->n_items = (int)items.size();
-  p->smem = smem;
   p->dirty = false;
   return GBNUTS_OK;
 }
@@ -406,7 +415,7 @@ int gbnuts_pool_submit(gbnuts_pool* p, int kind, const void* X, int x_dtype, con
   if (!p || !rc || !out || !fit_id || !y || N <= 0 || K < 0)
     return fail(GBNUTS_USAGE, "bad arguments");
   if (x_dtype != p->x_dtype) return fail(GBNUTS_USAGE, "x_dtype differs from the pool's");
-  if (chains_per_block(K) != 16) return fail(GBNUTS_USAGE, "the pool takes fits with K <= 512");
+  if (chains_per_block(K) == 0) return fail(GBNUTS_USAGE, "K above 2048 is not supported");
   if (rc->num_chains <= 0 || rc->num_chains > p->max_chains)
     return fail(GBNUTS_USAGE, "num_chains must be in 1..max_chains");
   if (!out->draws || !out->n_rows) return fail(GBNUTS_USAGE, "draws / n_rows buffers missing");
@@ -466,9 +475,12 @@ int gbnuts_pool_step(gbnuts_pool* p, int n_steps, int* n_running, int* n_queued)
       for (ActiveFit* f : p->active)
         if (f->memset_gz)
           cudaMemsetAsync(f->Gz, 0, (size_t)f->C * f->model->desc.J * 8, p->stream);
-      int rc = launch_partials_pool(p->d_gfits, p->d_items, p->n_items, p->x_dtype,
-                                    p->precision, p->smem, p->stream);
-      if (rc) return rc;
+      for (int k = 0; k < 3; ++k) {
+        int rc = launch_partials_pool(p->d_gfits, p->d_items + p->item_off[k], p->item_n[k],
+                                      4 << k, p->x_dtype, p->precision, p->smem_cb[k],
+                                      p->stream);
+        if (rc) return rc;
+      }
     }
     p->steps += n_steps;
     cudaError_t e = cudaMemcpyAsync(p->h_done, p->d_done, p->max_fits * sizeof(int),
