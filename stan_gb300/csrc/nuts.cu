@@ -28,6 +28,7 @@
 // explicit round-to-nearest operations so they round exactly like the host
 // oracle compiled without contraction.
 #include <math.h>
+#include <stdlib.h>
 
 #include "../../include/gbnuts.h"
 #include "../../include/gbnuts_draw_stream.h"
@@ -957,6 +958,16 @@ void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* sta
   const int threads = 128;
   const int blocks = (int)(((size_t)cfg.C * 32 + threads - 1) / threads);
   nuts_init_kernel<<<blocks, threads, 0, s>>>(cfg, states, stacks, vecs, inv_metrics, active);
+}
+
+int team_warps(int D) {
+  static const int forced = [] {
+    const char* e = getenv("GBNUTS_TEAM_WARPS");
+    const int w = e ? atoi(e) : 0;
+    return (w == 1 || w == 2 || w == 4) ? w : 0;
+  }();
+  if (forced) return forced;
+  return D <= 64 ? 1 : (D <= 1024 ? 2 : 4);
 }
 
 void launch_nuts_step_pool(const PoolFitDev* fits, const int2* chain_map, int total, int team,

@@ -106,9 +106,9 @@ struct PoolFitDev {
   FitPtrs f;
 };
 
-// Warps per chain of the step kernel for a dimension D (1, 2 or 4; measured
-// on the 1024-chain D = 101 and the 256-chain D = 2013 fits).
-inline int team_warps(int D) { return D <= 64 ? 1 : (D <= 1024 ? 2 : 4); }
+// Warps per chain of the step kernel for a dimension D: 1, 2 or 4 (1 up to
+// D = 64, 2 up to 1024; GBNUTS_TEAM_WARPS overrides it, for tuning).
+int team_warps(int D);
 
 // One step of `total` chains: chain_map[g] = (table index, chain in fit); all
 // of them with `team` warps per chain (team_warps of their fit's D).
