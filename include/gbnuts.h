@@ -282,6 +282,23 @@ int gbnuts_pool_status(gbnuts_pool* p, long long fit_id, int* state, int* rc);
 /* Steps run so far and chains admitted now. */
 int gbnuts_pool_stats(gbnuts_pool* p, long long* steps, long long* chains);
 
+/* ------------------------------------------------------------ diagnostics */
+
+/* Split rank-normalised bulk and tail ESS of n_quantities columns
+ * [col_begin, col_begin + n_quantities) of a draws array laid out like
+ * gbnuts_run_output.draws (num_chains x max_rows x n_cols), over rows
+ * [row_begin, row_begin + n_rows) of every chain
+ * (split_rank_normalized_ess.hpp:28-55).  out: 2 per quantity (bulk, tail;
+ * NaN where the reference returns NaN).  Computed on the device, one CTA per
+ * quantity, for up to 8192 split draws per quantity (2 x num_chains x
+ * floor(n_rows / 2)).  gbnuts_ess_device takes device buffers and a stream and
+ * is asynchronous; gbnuts_ess takes host buffers. */
+int gbnuts_ess_device(const double* d_draws, int num_chains, int max_rows, int n_cols,
+                      int row_begin, int n_rows, int col_begin, int n_quantities,
+                      double* d_out, void* stream);
+int gbnuts_ess(const double* draws, int num_chains, int max_rows, int n_cols, int row_begin,
+               int n_rows, int col_begin, int n_quantities, double* out);
+
 /* Device and build information: writes a short text description. */
 int gbnuts_device_info(char* buf, int cap);
 

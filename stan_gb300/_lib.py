@@ -111,6 +111,11 @@ SIGNATURES = {
     "gbnuts_pool_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _ip]),
     "gbnuts_pool_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, _ip, _ip]),
     "gbnuts_pool_stats": (ctypes.c_int, [ctypes.c_void_p, _llp, _llp]),
+    "gbnuts_ess_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_void_p]),
+    "gbnuts_ess": (ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
     "gbnuts_device_info": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "gbnuts_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
 }

@@ -107,3 +107,44 @@ def test_non_finite_density_is_reported_not_raised(models):
     th = np.full(m.D, 400.0)
     lp, g = m.log_prob_grad(th)
     assert not np.isfinite(lp)
+
+
+def test_full_size_hier_normal_config_c():
+    """J = 2000 groups (~42k rows), D = 2013: FP64 to 1e-12, FP32 within its
+    stated tolerance, against the oracle."""
+    from stan_gb300 import Model
+    ds = make_dataset("hier_normal", small=False, seed=1)
+    m = Model.from_dataset(ds)
+    om = ds.oracle_model()
+    C = 32
+    th = np.random.default_rng(8).normal(size=(C, m.D)) * 0.2
+    lp64, g64 = m.log_prob_grad_batch(th, "fp64")
+    lp32, g32 = m.log_prob_grad_batch(th, "fp32")
+    for c in (0, 7, 31):
+        lpo, go = om.log_prob_grad(th[c])
+        assert abs(lp64[c] - lpo) <= 1e-12 * abs(lpo)
+        assert np.linalg.norm(g64[c] - go) <= 1e-12 * np.linalg.norm(go)
+        assert abs(lp32[c] - lpo) <= 1e-5 * abs(lpo)
+        assert np.linalg.norm(g32[c] - go) <= 1e-4 * np.linalg.norm(go)
+
+
+def test_full_size_poisson_config_d():
+    """N = 262144, K = 512, X stored bf16: FP64 to 1e-12 against the oracle;
+    the bf16 tensor-core forms within their stated tolerances."""
+    from stan_gb300 import Model
+    ds = make_dataset("poisson", small=False, seed=1)
+    m = Model.from_dataset(ds)
+    om = ds.oracle_model()
+    C = 16
+    th = np.random.default_rng(9).normal(size=(C, m.D)) * 0.05
+    lp64, g64 = m.log_prob_grad_batch(th, "fp64")
+    lp3, g3 = m.log_prob_grad_batch(th, "bf16x3")
+    lp1, g1 = m.log_prob_grad_batch(th, "bf16")
+    for c in (0, 15):
+        lpo, go = om.log_prob_grad(th[c])
+        assert abs(lp64[c] - lpo) <= 1e-12 * abs(lpo)
+        assert np.linalg.norm(g64[c] - go) <= 1e-12 * np.linalg.norm(go)
+        assert abs(lp3[c] - lpo) <= 1e-5 * abs(lpo)
+        assert np.linalg.norm(g3[c] - go) <= 1e-4 * np.linalg.norm(go)
+        assert abs(lp1[c] - lpo) <= 1e-3 * abs(lpo)
+        assert np.linalg.norm(g1[c] - go) <= 1e-2 * np.linalg.norm(go)
