@@ -343,7 +343,8 @@ def serving_leg(n_fits=None, rate=None, forms=("fp32", "fp64")):
     """Continuous batching on the serving stream (N log-uniform in [200, 5e4],
     K in {8, ..., 128}, data at prior draws, 4 chains, 300 + 500): fits
     arrive as a Poisson process and run in one pool per form; p50 / p99
-    latency (arrival to every draw on the host) and fits/s, for the mixed
+    latency (arrival to every draw and its on-device ESS report on the host) and
+    fits/s, for the mixed
     (fp32 gradients, FP64 control) and the plain FP64 form."""
     from stan_gb300 import workloads
     from stan_gb300.serving import Pool, poisson_arrivals, serve
@@ -352,20 +353,25 @@ def serving_leg(n_fits=None, rate=None, forms=("fp32", "fp64")):
     rate = rate or S["rate"]
     dss = workloads.serving_stream(n_fits)
     kw = dict(num_chains=S["chains"], num_warmup=S["warmup"], num_samples=S["samples"],
-              random_seed=1, max_depth=10, delta=0.8)
+              random_seed=1, max_depth=10, delta=0.8, report_ess=True)
     arrivals = poisson_arrivals(rate, len(dss), seed=1)
     out = {"workload": f"{n_fits} hierarchical logistic fits (N log-uniform 200-50000, K in "
                        f"8/16/32/64/128, J = N/50, y at prior draws), {S['chains']} chains, "
                        f"{S['warmup']} warmup + {S['samples']} draws",
            "arrival_rate_per_s": rate, "latency_unit": "s",
-           "latency": "arrival to the fit's draws in host memory"}
+           "latency": "arrival to the fit's draws and ESS report in host memory"}
     for form in forms:
         pool = Pool(precision=form, x_dtype="f32", max_fits=512, reserve_bytes=2 << 30)
         pool.submit(dss[0], **dict(kw, num_warmup=20, num_samples=0))  # warm-up fit
         pool.run_all()
-        rep = serve(pool, dss, arrivals, steps_per_call=S["steps_per_call"], run_kwargs=kw)
+        ess = {}
+        rep = serve(pool, dss, arrivals, steps_per_call=S["steps_per_call"], run_kwargs=kw,
+                    on_done=lambda i, r: ess.__setitem__(i, float(np.nanmin(r.ess[:, 0]))))
         pool.close()
-        out["mixed" if form == "fp32" else "fp64"] = rep.summary()
+        summ = rep.summary()
+        # convergence report computed on the device as each fit retires
+        summ["min_bulk_ess_median_over_fits"] = float(np.median(list(ess.values())))
+        out["mixed" if form == "fp32" else "fp64"] = summ
     return out
 
 

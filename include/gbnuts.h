@@ -228,6 +228,11 @@ typedef struct {
   double grad_ms;         /* time in the gradient kernels, CUDA events */
   long long steps;        /* batched gradient steps launched */
   long long kernel_launches;
+  /* NULL, or 2 x (1 + D) doubles: split rank-normalised (bulk, tail) ESS of
+   * lp__ then of each parameter over the post-warmup draws, computed on the
+   * device before the draws are copied out (NaN when a fit has more than 8192
+   * split draws per quantity, or where the reference gives NaN). */
+  double* ess;
 } gbnuts_run_output;
 
 /* Chain status codes. */

@@ -59,7 +59,8 @@ class RunOutput(ctypes.Structure):
                 ("diagnostics", _dp), ("n_rows", _ip), ("n_warmup_rows", _ip), ("status", _ip),
                 ("stepsize", _dp), ("inv_metric", _dp), ("init", _dp), ("n_grad", _llp),
                 ("seconds", _dp), ("total_ms", ctypes.c_double), ("grad_ms", ctypes.c_double),
-                ("steps", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong)]
+                ("steps", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong),
+                ("ess", _dp)]
 
 
 # Every exported symbol and its signature (restype, argtypes).

@@ -285,6 +285,32 @@ extern "C" int gbnuts_ess_device(const double* d_draws, int num_chains, int max_
   return GBNUTS_OK;
 }
 
+namespace gbn {
+int fit_ess(const double* d_draws, int C, int max_rows, int n_cols, int row_begin, int n_rows,
+            double* h_out, cudaStream_t st) {
+  const int nq = 1 + (n_cols - 7);
+  for (int i = 0; i < 2 * nq; ++i) h_out[i] = nan("");
+  if (n_rows < 8 || 2 * C > 1024 || 2 * C * (n_rows / 2) > kMaxValues) return GBNUTS_OK;
+  double* d_out = nullptr;
+  GBN_CUDA_TRY(cudaMalloc(&d_out, (size_t)2 * nq * sizeof(double)));
+  int rc = gbnuts_ess_device(d_draws, C, max_rows, n_cols, row_begin, n_rows, 0, 1, d_out, st);
+  if (rc == GBNUTS_OK && nq > 1)
+    rc = gbnuts_ess_device(d_draws, C, max_rows, n_cols, row_begin, n_rows, 7, nq - 1, d_out + 2,
+                           st);
+  cudaError_t e = cudaSuccess;
+  if (rc == GBNUTS_OK)
+    e = cudaMemcpyAsync(h_out, d_out, (size_t)2 * nq * sizeof(double), cudaMemcpyDeviceToHost,
+                        st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_out);
+  if (e != cudaSuccess) {
+    set_last_error(std::string("fit ESS: ") + cudaGetErrorString(e));
+    return GBNUTS_SOFTWARE;
+  }
+  return rc;
+}
+}  // namespace gbn
+
 extern "C" int gbnuts_ess(const double* draws, int num_chains, int max_rows, int n_cols,
                           int row_begin, int n_rows, int col_begin, int n_quantities,
                           double* out) {

@@ -123,6 +123,12 @@ int launch_partials_pool(const PoolGradFit* d_fits, const PoolWorkItem* d_items,
 // Maximum chains per block of the partial kernel for a given K (0 if K is
 // beyond what the kernel supports).
 int chains_per_block(int K);
+// Device ESS of a finished fit's draws into host out[2 x (1 + D)] (lp__ then
+// the parameters; rows [row_begin, row_begin + n_rows)); NaN when the fit is
+// too large for the on-device form.
+int fit_ess(const double* d_draws, int C, int max_rows, int n_cols, int row_begin, int n_rows,
+            double* h_out, cudaStream_t st);
+
 // Chains per block a fit of C chains uses (the smaller of chains_per_block(K)
 // and C rounded up to 4, 8 or 16): fewer idle threads for small fits.
 int block_chains(int K, int C);

@@ -60,3 +60,25 @@ def test_fit_report_matches_host():
     for k in range(q.shape[2]):
         b, t = analyze.split_rank_normalized_ess(q[:, :, k])
         assert abs(bulk[k] - b) <= 1e-8 * b and abs(tail[k] - t) <= 1e-8 * t, k
+
+
+def test_run_reports_ess_alone_and_in_pool():
+    """RunResult.ess (computed on the device at the end of the run) equals the
+    host restatement, for an alone run and the same fit inside a pool."""
+    from stan_gb300 import Model, analyze, sampler
+    from stan_gb300.serving import Pool
+    from tests.datasets import make_dataset
+    ds = make_dataset("hier_normal", small=True, seed=5)
+    kw = dict(num_chains=4, num_warmup=150, num_samples=200, random_seed=6, report_ess=True)
+    r = sampler.run(Model.from_dataset(ds, x_dtype="f32"), precision="fp32", **kw)
+    d = r.sampling_draws()
+    q = np.concatenate([d[:, :, 0:1], d[:, :, 7:]], axis=2)
+    for k in range(q.shape[2]):
+        b, t = analyze.split_rank_normalized_ess(q[:, :, k])
+        assert abs(r.ess[k, 0] - b) <= 1e-8 * b and abs(r.ess[k, 1] - t) <= 1e-8 * t, k
+    pool = Pool(precision="fp32", x_dtype="f32", reserve_bytes=0)
+    fid = pool.submit(ds, **kw)
+    pool.run_all()
+    rp = pool.pop(fid)
+    assert np.array_equal(rp.ess, r.ess)
+    pool.close()
