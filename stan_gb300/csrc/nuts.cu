@@ -903,7 +903,7 @@ __global__ void __launch_bounds__(W == 1 ? 128 : 32 * W, 1)
   const int t = (W == 1) ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   const int k = (W == 1) ? (int)(threadIdx.x >> 5) : 0;
   if (g >= total) return;  // uniform per team
-  const Team tm{t, 32 * W, W, sh_red};
+  const Team tm{t, 32 * W, W, sh_red, 1};
   const int2 fc = chain_map[g];
   const unsigned long long* src = reinterpret_cast<const unsigned long long*>(fits + fc.x);
   unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sh_fit[k]);

@@ -102,6 +102,10 @@ struct gbnuts_pool {
   long long max_chains = 0;
   long long reserve_bytes = 0;
   cudaStream_t stream = nullptr;
+  // side streams and events: launches of different classes (team size, chains
+  // per block) of the same step run concurrently
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
   int* d_done = nullptr;
   int* d_abort = nullptr;
   int* h_done = nullptr;  // pinned
@@ -387,6 +391,11 @@ int gbnuts_pool_create(int precision, int x_dtype, int max_fits, long long max_c
   p->max_chains = max_chains;
   p->reserve_bytes = reserve_bytes;
   cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+    e = cudaStreamCreateWithFlags(&p->side[i], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_join[i], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&p->d_done, max_fits * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&p->d_abort, max_fits * sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(p->d_abort, 0, max_fits * sizeof(int));
@@ -414,6 +423,11 @@ void gbnuts_pool_destroy(gbnuts_pool* p) {
   if (p->d_done) cudaFree(p->d_done);
   if (p->d_abort) cudaFree(p->d_abort);
   if (p->h_done) cudaFreeHost(p->h_done);
+  for (int i = 0; i < 2; ++i) {
+    if (p->side[i]) cudaStreamDestroy(p->side[i]);
+    if (p->ev_join[i]) cudaEventDestroy(p->ev_join[i]);
+  }
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->stream) cudaStreamDestroy(p->stream);
   delete p;
 }
@@ -478,19 +492,43 @@ int gbnuts_pool_step(gbnuts_pool* p, int n_steps, int* n_running, int* n_queued)
     if (rc) return rc;
   }
   if (!p->active.empty() && n_steps > 0) {
+    // Launches of the present classes: the first on the pool's stream, the
+    // others on side streams forked from it and joined back.
+    auto classes = [&](const int* counts, auto&& launch) -> int {
+      int present = 0;
+      for (int k = 0; k < 3; ++k) present += counts[k] > 0;
+      bool first = true;
+      int side = 0;
+      if (present > 1) cudaEventRecord(p->ev_fork, p->stream);
+      for (int k = 0; k < 3; ++k) {
+        if (counts[k] == 0) continue;
+        cudaStream_t st = p->stream;
+        if (!first) {
+          st = p->side[side];
+          cudaStreamWaitEvent(st, p->ev_fork, 0);
+        }
+        const int rc = launch(k, st);
+        if (rc) return rc;
+        if (!first) cudaEventRecord(p->ev_join[side++], st);
+        first = false;
+      }
+      for (int i = 0; i < side; ++i) cudaStreamWaitEvent(p->stream, p->ev_join[i], 0);
+      return GBNUTS_OK;
+    };
     for (int k = 0; k < n_steps; ++k) {
-      for (int k = 0; k < 3; ++k)
-        launch_nuts_step_pool(p->d_fits, p->d_chain_map + p->team_off[k], p->team_n[k], 1 << k,
-                              p->stream);
+      classes(p->team_n, [&](int c, cudaStream_t st) {
+        launch_nuts_step_pool(p->d_fits, p->d_chain_map + p->team_off[c], p->team_n[c], 1 << c,
+                              st);
+        return GBNUTS_OK;
+      });
       for (ActiveFit* f : p->active)
         if (f->memset_gz)
           cudaMemsetAsync(f->Gz, 0, (size_t)f->C * f->model->desc.J * 8, p->stream);
-      for (int k = 0; k < 3; ++k) {
-        int rc = launch_partials_pool(p->d_gfits, p->d_items + p->item_off[k], p->item_n[k],
-                                      4 << k, p->x_dtype, p->precision, p->smem_cb[k],
-                                      p->stream);
-        if (rc) return rc;
-      }
+      const int rc = classes(p->item_n, [&](int c, cudaStream_t st) {
+        return launch_partials_pool(p->d_gfits, p->d_items + p->item_off[c], p->item_n[c],
+                                    4 << c, p->x_dtype, p->precision, p->smem_cb[c], st);
+      });
+      if (rc) return rc;
     }
     p->steps += n_steps;
     cudaError_t e = cudaMemcpyAsync(p->h_done, p->d_done, p->max_fits * sizeof(int),

@@ -1,6 +1,6 @@
-// The threads that run one chain of the sampler: one warp (four chains per
-// CTA) for small dimensions, or a whole CTA of two or four warps for large
-// ones.  Every thread of a team holds the chain's scalar state and executes
+// The threads that run one chain of the sampler: one warp for small
+// dimensions (four chains per CTA), or a CTA of two or four warps for large
+// ones (synchronising on a named barrier).  Every thread of a team holds the chain's scalar state and executes
 // the same control flow; vector work is strided over the team's threads;
 // reductions combine the warps' butterfly sums in warp order (deterministic
 // for a given team size).
@@ -11,14 +11,18 @@ namespace gbn {
 struct Team {
   int t;        // thread index within the team
   int n;        // team size: 32 * nw
-  int nw;       // warps in the team (1, or the whole CTA)
+  int nw;       // warps in the team
   double* red;  // shared scratch, 8 doubles per warp (nw > 1)
+  int bar;      // named barrier of a multi-warp team (1 or 2)
 
+  // Barrier ids are immediates so a kernel reserves only barriers 0-2.
   __device__ __forceinline__ void sync() const {
     if (nw == 1)
       __syncwarp();
+    else if (bar == 1)
+      asm volatile("barrier.cta.sync 1, %0;" ::"r"(n) : "memory");
     else
-      __syncthreads();
+      asm volatile("barrier.cta.sync 2, %0;" ::"r"(n) : "memory");
   }
 
   __device__ __forceinline__ double sum(double v) const {
@@ -26,10 +30,10 @@ struct Team {
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     if (nw == 1) return v;
     if ((t & 31) == 0) red[(t >> 5) * 8] = v;
-    __syncthreads();
+    sync();
     double s = 0.0;
     for (int w = 0; w < nw; ++w) s += red[w * 8];
-    __syncthreads();
+    sync();
     return s;
   }
 
@@ -43,19 +47,38 @@ struct Team {
     if ((t & 31) == 0)
 #pragma unroll
       for (int j = 0; j < 6; ++j) red[(t >> 5) * 8 + j] = v[j];
-    __syncthreads();
+    sync();
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
       double s = 0.0;
       for (int w = 0; w < nw; ++w) s += red[w * 8 + j];
       v[j] = s;
     }
-    __syncthreads();
+    sync();
   }
 
   __device__ __forceinline__ bool any(bool b) const {
     if (nw == 1) return __any_sync(0xffffffffu, b) != 0;
-    return __syncthreads_or(b) != 0;
+    unsigned r;
+    if (bar == 1)
+      asm volatile(
+          "{\n\t.reg .pred q, o;\n\t"
+          "setp.ne.u32 q, %1, 0;\n\t"
+          "barrier.cta.red.or.pred o, 1, %2, q;\n\t"
+          "selp.u32 %0, 1, 0, o;\n\t}\n"
+          : "=r"(r)
+          : "r"((unsigned)b), "r"(n)
+          : "memory");
+    else
+      asm volatile(
+          "{\n\t.reg .pred q, o;\n\t"
+          "setp.ne.u32 q, %1, 0;\n\t"
+          "barrier.cta.red.or.pred o, 2, %2, q;\n\t"
+          "selp.u32 %0, 1, 0, o;\n\t}\n"
+          : "=r"(r)
+          : "r"((unsigned)b), "r"(n)
+          : "memory");
+    return r != 0;
   }
 };
 
