@@ -343,7 +343,8 @@ def serving_leg(n_fits=None, rate=None, forms=("fp32", "fp64")):
     """Continuous batching on the serving stream (N log-uniform in [200, 5e4],
     K in {8, ..., 128}, data at prior draws, 4 chains, 300 + 500): fits
     arrive as a Poisson process and run in one pool per form; p50 / p99
-    latency (arrival to every draw and its on-device ESS report on the host) and
+    latency (arrival to every draw and its on-device convergence summary (ESS,
+    R-hat, MCSE) on the host) and
     fits/s, for the mixed
     (fp32 gradients, FP64 control) and the plain FP64 form."""
     from stan_gb300 import workloads
@@ -353,24 +354,32 @@ def serving_leg(n_fits=None, rate=None, forms=("fp32", "fp64")):
     rate = rate or S["rate"]
     dss = workloads.serving_stream(n_fits)
     kw = dict(num_chains=S["chains"], num_warmup=S["warmup"], num_samples=S["samples"],
-              random_seed=1, max_depth=10, delta=0.8, report_ess=True)
+              random_seed=1, max_depth=10, delta=0.8, report_summary=True)
     arrivals = poisson_arrivals(rate, len(dss), seed=1)
     out = {"workload": f"{n_fits} hierarchical logistic fits (N log-uniform 200-50000, K in "
                        f"8/16/32/64/128, J = N/50, y at prior draws), {S['chains']} chains, "
                        f"{S['warmup']} warmup + {S['samples']} draws",
            "arrival_rate_per_s": rate, "latency_unit": "s",
-           "latency": "arrival to the fit's draws and ESS report in host memory"}
+           "latency": "arrival to the fit's draws and convergence summary (ESS, R-hat, MCSE) "
+                      "in host memory"}
     for form in forms:
         pool = Pool(precision=form, x_dtype="f32", max_fits=512, reserve_bytes=2 << 30)
         pool.submit(dss[0], **dict(kw, num_warmup=20, num_samples=0))  # warm-up fit
         pool.run_all()
-        ess = {}
+        ess, rhat = {}, {}
+
+        def done(i, r):
+            ess[i] = float(np.nanmin(r.summary[:, 0]))
+            rhat[i] = float(np.nanmax(r.summary[:, 2:4]))
+
         rep = serve(pool, dss, arrivals, steps_per_call=S["steps_per_call"], run_kwargs=kw,
-                    on_done=lambda i, r: ess.__setitem__(i, float(np.nanmin(r.ess[:, 0]))))
+                    on_done=done)
         pool.close()
         summ = rep.summary()
         # convergence report computed on the device as each fit retires
         summ["min_bulk_ess_median_over_fits"] = float(np.median(list(ess.values())))
+        summ["max_rhat_median_over_fits"] = float(np.median(list(rhat.values())))
+        summ["max_rhat_max_over_fits"] = float(np.max(list(rhat.values())))
         out["mixed" if form == "fp32" else "fp64"] = summ
     return out
 
@@ -473,6 +482,8 @@ def main():
     ap.add_argument("--no-config-d", action="store_true")
     ap.add_argument("--serving-fits", type=int, default=None)
     ap.add_argument("--serving-rate", type=float, default=None)
+    ap.add_argument("--serving-forms", default="fp32,fp64",
+                    help="comma list of the serving leg's gradient forms (fp32: mixed)")
     ap.add_argument("--case", default="fit", choices=["fit", "grad", "shortfit", "serving"],
                     help="fit: the benchmark; grad: two batched-gradient launches of the "
                          "workload (for kernel captures); shortfit: a fit of --short-iters "
@@ -480,7 +491,8 @@ def main():
     ap.add_argument("--short-iters", type=int, default=40)
     args = ap.parse_args()
     if args.case == "serving":
-        print(json.dumps(serving_leg(args.serving_fits, args.serving_rate)))
+        print(json.dumps(serving_leg(args.serving_fits, args.serving_rate,
+                                     tuple(args.serving_forms.split(",")))))
         return
     if args.case != "fit":
         profile_case(args)

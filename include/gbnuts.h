@@ -233,6 +233,11 @@ typedef struct {
    * device before the draws are copied out (NaN when a fit has more than 8192
    * split draws per quantity, or where the reference gives NaN). */
   double* ess;
+  /* NULL, or 6 x (1 + D) doubles: per quantity (lp__ then each parameter)
+   * bulk ESS, tail ESS, bulk R-hat, tail R-hat, mcse_mean, mcse_sd, as
+   * gbnuts_summary_device computes them over the post-warmup draws (NaN when
+   * the fit holds more than 8192 post-warmup draws per quantity). */
+  double* summary;
 } gbnuts_run_output;
 
 /* Chain status codes. */
@@ -303,6 +308,18 @@ int gbnuts_ess_device(const double* d_draws, int num_chains, int max_rows, int n
                       double* d_out, void* stream);
 int gbnuts_ess(const double* draws, int num_chains, int max_rows, int n_cols, int row_begin,
                int n_rows, int col_begin, int n_quantities, double* out);
+
+/* The same columns' full convergence summary, out: 6 per quantity
+ *   bulk ESS, tail ESS      split_rank_normalized_ess.hpp:28-55
+ *   bulk R-hat, tail R-hat  split_rank_normalized_rhat.hpp:28-45 (rhat.hpp:20-45)
+ *   mcse_mean, mcse_sd      mcse.hpp:22-61 (on the unsplit chains)
+ * NaN where the reference returns NaN.  For up to 8192 draws per quantity
+ * (num_chains x n_rows) and 512 chains.  Device and host-buffer forms as above. */
+int gbnuts_summary_device(const double* d_draws, int num_chains, int max_rows, int n_cols,
+                          int row_begin, int n_rows, int col_begin, int n_quantities,
+                          double* d_out, void* stream);
+int gbnuts_summary(const double* draws, int num_chains, int max_rows, int n_cols, int row_begin,
+                   int n_rows, int col_begin, int n_quantities, double* out);
 
 /* Device and build information: writes a short text description. */
 int gbnuts_device_info(char* buf, int cap);

@@ -60,7 +60,7 @@ class RunOutput(ctypes.Structure):
                 ("stepsize", _dp), ("inv_metric", _dp), ("init", _dp), ("n_grad", _llp),
                 ("seconds", _dp), ("total_ms", ctypes.c_double), ("grad_ms", ctypes.c_double),
                 ("steps", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong),
-                ("ess", _dp)]
+                ("ess", _dp), ("summary", _dp)]
 
 
 # Every exported symbol and its signature (restype, argtypes).
@@ -117,6 +117,13 @@ SIGNATURES = {
                                          ctypes.c_void_p, ctypes.c_void_p]),
     "gbnuts_ess": (ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
+    "gbnuts_summary_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p]),
+    "gbnuts_summary": (ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      _dp]),
     "gbnuts_device_info": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "gbnuts_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
 }

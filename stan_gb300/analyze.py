@@ -9,6 +9,8 @@ stan-dev/stan tree):
   src/stan/analyze/mcmc/check_chains.hpp                is_finite_and_varies
   src/stan/analyze/mcmc/split_rank_normalized_ess.hpp:28-55   (bulk, tail)
   src/stan/analyze/mcmc/mcse.hpp:22-61                  mcse_mean, mcse_sd
+  src/stan/analyze/mcmc/rhat.hpp:20-45                  rhat from W and B
+  src/stan/analyze/mcmc/split_rank_normalized_rhat.hpp:28-45  (bulk, tail) R-hat
 The normal quantile is scipy.special.ndtri (the reference uses Boost's
 quantile(normal)); the sample quantile is the linear-interpolation (R type 7)
 estimator of Stan Math's quantile().  Chains are the columns of a
@@ -132,6 +134,28 @@ def split_rank_normalized_ess(chains):
         tail = e05
     else:
         tail = min(e05, e95)
+    return bulk, tail
+
+
+def rhat(chains):
+    """sqrt(((n - 1)/n W + B/n) / W) with B, W the between- and within-chain variances."""
+    chains = np.asarray(chains, dtype=np.float64)
+    n, m = chains.shape
+    means = chains.mean(axis=0)
+    b = n * ((means - means.mean()) ** 2).sum() / (m - 1)
+    w = (((chains - means) ** 2).sum(axis=0) / (n - 1.0)).sum() / m
+    return math.sqrt((b / w + n - 1) / n)
+
+
+def split_rank_normalized_rhat(chains):
+    """(bulk R-hat, tail R-hat) of one quantity: R-hat of the normal scores of the
+    split draws and of their distances from the median."""
+    sp = split_chains(chains)
+    if not is_finite_and_varies(sp):
+        return float("nan"), float("nan")
+    bulk = rhat(rank_transform(sp))
+    med = quantile(sp.reshape(-1, order="F"), 0.5)
+    tail = rhat(rank_transform(np.abs(sp - med)))
     return bulk, tail
 
 

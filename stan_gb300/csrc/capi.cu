@@ -736,14 +736,15 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
 
   std::vector<ChainState> hs(C);
   GBN_CUDA_TRY(cudaMemcpy(hs.data(), d_states, C * sizeof(ChainState), cudaMemcpyDeviceToHost));
-  if (out->ess) {
+  if (out->ess || out->summary) {
     // convergence report on the device, before the draws leave it
     int w = 0, nr = out->max_rows;
     for (int c = 0; c < C; ++c) {
       w = std::max(w, hs[c].warm_rows);
       nr = std::min(nr, hs[c].rows);
     }
-    const int re = fit_ess(d_draws, C, out->max_rows, n_cols, w, std::max(0, nr - w), out->ess, st);
+    const int re = fit_ess(d_draws, C, out->max_rows, n_cols, w, std::max(0, nr - w), out->ess,
+                           out->summary, st);
     if (re) return re;
   }
   GBN_CUDA_TRY(cudaMemcpy(out->draws, d_draws, (size_t)C * out->max_rows * n_cols * sizeof(double),

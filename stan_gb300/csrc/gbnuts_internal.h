@@ -123,11 +123,12 @@ int launch_partials_pool(const PoolGradFit* d_fits, const PoolWorkItem* d_items,
 // Maximum chains per block of the partial kernel for a given K (0 if K is
 // beyond what the kernel supports).
 int chains_per_block(int K);
-// Device ESS of a finished fit's draws into host out[2 x (1 + D)] (lp__ then
-// the parameters; rows [row_begin, row_begin + n_rows)); NaN when the fit is
-// too large for the on-device form.
+// Device convergence report of a finished fit's draws (lp__ then the
+// parameters; rows [row_begin, row_begin + n_rows)): ESS pairs into host
+// h_ess[2 x (1 + D)] and/or six-value summaries into h_summary[6 x (1 + D)]
+// (either may be null); NaN when the fit is too large for the on-device form.
 int fit_ess(const double* d_draws, int C, int max_rows, int n_cols, int row_begin, int n_rows,
-            double* h_out, cudaStream_t st);
+            double* h_ess, double* h_summary, cudaStream_t st);
 
 // Chains per block a fit of C chains uses (the smaller of chains_per_block(K)
 // and C rounded up to 4, 8 or 16): fewer idle threads for small fits.

@@ -251,7 +251,7 @@ static int retire(gbnuts_pool* p, ActiveFit* f) {
     e = cudaMemcpy2D(out->inv_metric, D * 8, f->vecs + (size_t)SL_INVM * cfg.ld,
                      (size_t)cfg.n_slots * cfg.ld * 8, D * 8, C, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) rc = fail(GBNUTS_SOFTWARE, std::string("fit readback: ") + cudaGetErrorString(e));
-  if (rc == GBNUTS_OK && out->ess) {
+  if (rc == GBNUTS_OK && (out->ess || out->summary)) {
     // convergence report on the device, before the fit's memory is freed
     int w = 0, nr = out->max_rows;
     for (int c = 0; c < C; ++c) {
@@ -259,7 +259,7 @@ static int retire(gbnuts_pool* p, ActiveFit* f) {
       nr = std::min(nr, hs[c].rows);
     }
     rc = fit_ess(f->draws, C, out->max_rows, cfg.n_cols, w, std::max(0, nr - w), out->ess,
-                 p->stream);
+                 out->summary, p->stream);
   }
   const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - f->admitted).count();
   for (int c = 0; c < C && rc == GBNUTS_OK; ++c) {

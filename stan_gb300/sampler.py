@@ -8,6 +8,7 @@ from . import _lib
 
 SAMPLER_COLUMNS = ["lp__", "accept_stat__", "stepsize__", "treedepth__", "n_leapfrog__",
                    "divergent__", "energy__"]
+SUMMARY_COLUMNS = ["ess_bulk", "ess_tail", "rhat_bulk", "rhat_tail", "mcse_mean", "mcse_sd"]
 _dp = ctypes.POINTER(ctypes.c_double)
 
 
@@ -32,6 +33,8 @@ class RunResult:
     kernel_launches: int
     diagnostics: np.ndarray = None
     ess: np.ndarray = None   # (1 + D, 2): bulk, tail ESS of lp__ and each parameter
+    # (1 + D, 6): bulk ESS, tail ESS, bulk R-hat, tail R-hat, mcse_mean, mcse_sd
+    summary: np.ndarray = None
 
     def sampling_draws(self):
         """(iterations, chains, 7 + D) post-warmup draws (the chainset layout)."""
@@ -44,11 +47,14 @@ def prepare(D, num_chains=4, adapt=True, num_warmup=1000, num_samples=1000, num_
             save_warmup=False, stepsize=1.0, stepsize_jitter=0.0, max_depth=10, delta=0.8,
             gamma=0.05, kappa=0.75, t0=10.0, init_buffer=75, term_buffer=50, window=25,
             init_radius=2.0, random_seed=0, init_chain_id=1, precision="fp64",
-            inits=None, inv_metrics=None, save_diagnostics=False, report_ess=False):
+            inits=None, inv_metrics=None, save_diagnostics=False, report_ess=False,
+            report_summary=False):
     """Run configuration and caller-owned output buffers for a fit of dimension D.
 
     report_ess: also compute the split rank-normalised bulk / tail ESS of every
     quantity on the device when the fit ends (RunResult.ess).
+    report_summary: also the full convergence summary (ESS, R-hat, MCSE) of every
+    quantity, on the device (RunResult.summary; SUMMARY_COLUMNS).
 
     Returns (config, output, result): the ctypes structures point into the
     arrays of `result`, which must stay alive until the run has written them.
@@ -73,6 +79,8 @@ def prepare(D, num_chains=4, adapt=True, num_warmup=1000, num_samples=1000, num_
                     np.zeros((C, rows, 3 * D)) if save_diagnostics else None)
     if report_ess:
         res.ess = np.full((1 + D, 2), np.nan)
+    if report_summary:
+        res.summary = np.full((1 + D, 6), np.nan)
     res._keep = (ini, imi)
     ip = ctypes.POINTER(ctypes.c_int)
     out = _lib.RunOutput(rows, ncol, _ptr(res.draws),
@@ -81,7 +89,8 @@ def prepare(D, num_chains=4, adapt=True, num_warmup=1000, num_samples=1000, num_
                          res.status.ctypes.data_as(ip), _ptr(res.stepsize), _ptr(res.inv_metric),
                          _ptr(res.init), res.n_grad.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
                          _ptr(res.seconds), 0.0, 0.0, 0, 0,
-                         None if res.ess is None else _ptr(res.ess))
+                         None if res.ess is None else _ptr(res.ess),
+                         None if res.summary is None else _ptr(res.summary))
     return cfg, out, res
 
 

@@ -59,3 +59,22 @@ def test_min_bulk_ess(bern):
     d = np.stack([bern["lp"], bern["theta"]], axis=2)
     v, name = A.min_bulk_ess(d, ["lp__", "theta"])
     assert name == "theta" and v == pytest.approx(1407.5124, abs=1e-4)
+
+
+def test_split_rank_normalized_rhat(bern):
+    # split_rank_normalized_rhat_test.cpp:40-52 (computed by R posterior; 1e-5)
+    lp = A.split_rank_normalized_rhat(bern["lp"])
+    th = A.split_rank_normalized_rhat(bern["theta"])
+    assert max(lp) == pytest.approx(1.00073, abs=1e-5)
+    assert max(th) == pytest.approx(1.006789, abs=1e-5)
+    # split_rank_normalized_rhat_test.cpp:54-66
+    assert all(np.isnan(A.split_rank_normalized_rhat(bern["divergent"])))
+    bad = bern["theta"].copy()
+    bad[0, 0] = np.inf
+    assert all(np.isnan(A.split_rank_normalized_rhat(bad)))
+
+
+def test_rhat_identical_chains_is_below_one():
+    # rhat of chains with equal means: B = 0, so sqrt((n - 1) / n)
+    x = np.tile(np.arange(10.0)[:, None], (1, 3))
+    assert A.rhat(x) == pytest.approx(np.sqrt(9 / 10), abs=1e-15)
