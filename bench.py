@@ -242,6 +242,11 @@ def run_ours(args, ws, rank, local):
             "min_bulk_ess_per_s_estimate"]
         if args.precision != "fp64":
             out["precision_errors"] = precision_errors(model, last, args.precision)
+    if rank == 0 and not args.no_csv:
+        try:
+            out["csv_output"] = csv_leg(model, last)
+        except Exception as e:  # reported, not fatal to the headline line
+            out["csv_output"] = {"error": repr(e)}
     if rank == 0 and not args.no_config_d:
         try:
             out["config_d"] = config_d_leg()
@@ -324,6 +329,43 @@ def config_d_leg():
                                                  np.linalg.norm(g64, axis=1)))
     m.close()
     return out
+
+
+def csv_leg(model, res, chains=256):
+    """Stan CSV output of the headline fit through the native writer
+    (gbnuts_write_run with gbnuts_csv_open's callbacks: the service protocol,
+    values at 6 significant digits) for its first `chains` chains, written to a
+    temporary directory and removed: once with the chains formatted
+    concurrently on the host cores and once on one thread."""
+    import ctypes
+    import shutil
+    import tempfile
+    from stan_gb300 import _lib
+    from stan_gb300.callbacks import CsvFiles
+    cfg, out = res._run
+    sub = type(cfg).from_buffer_copy(cfg)
+    sub.num_chains = min(chains, cfg.num_chains)
+    rows = int(res.n_rows[:sub.num_chains].sum())
+    report = {"chains": int(sub.num_chains), "rows": rows, "columns": int(out.n_cols),
+              "host_threads": os.cpu_count()}
+    for label, concurrent in (("concurrent", 1), ("one_thread", 0)):
+        d = tempfile.mkdtemp(prefix="gbnuts_csv_")
+        try:
+            csv = CsvFiles(os.path.join(d, "out"))
+            t0 = time.perf_counter()
+            cb = csv.open(sub.num_chains, sub.init_chain_id)
+            cb.chains_concurrent = concurrent
+            rc = _lib.load().gbnuts_write_run(model.handle, ctypes.byref(sub), ctypes.byref(out),
+                                              ctypes.byref(cb))
+            csv.close()
+            dt = time.perf_counter() - t0
+            _lib.check(rc, "gbnuts_write_run")
+            nbytes = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d))
+        finally:
+            shutil.rmtree(d, ignore_errors=True)
+        report[label] = {"seconds": dt, "bytes": nbytes, "MB_per_s": nbytes / dt / 1e6,
+                         "rows_per_s": rows / dt}
+    return report
 
 
 def fp64_rate(model, ds, C):
@@ -480,6 +522,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-config-d", action="store_true")
+    ap.add_argument("--no-csv", action="store_true")
     ap.add_argument("--serving-fits", type=int, default=None)
     ap.add_argument("--serving-rate", type=float, default=None)
     ap.add_argument("--serving-forms", default="fp32,fp64",

@@ -147,8 +147,12 @@ enum { GBNUTS_DEBUG = 0, GBNUTS_INFO = 1, GBNUTS_WARN = 2, GBNUTS_ERROR = 3, GBN
  * write_blank; logger.{debug..fatal} is log; interrupt() returning nonzero
  * aborts (the interface throwing from interrupt, generate_transitions.hpp:52);
  * structured_writer's {stepsize, metric_type, inv_metric} record
- * (base_hmc.hpp:70-76) is write_metric.  Callbacks run on the calling thread,
- * chain by chain in chain order, after the device run. */
+ * (base_hmc.hpp:70-76) is write_metric.  Callbacks run after the device run,
+ * chain by chain in chain order on the calling thread; or, when
+ * chains_concurrent is nonzero, the writers of different chains may be called
+ * from different threads at once (each chain's calls stay in order on one
+ * thread, as in the reference's per-chain TBB tasks), and log must then be
+ * thread-safe. */
 typedef struct {
   void* ctx;
   void (*write_names)(void* ctx, int chain, int writer, const char* const* names, int n);
@@ -160,7 +164,24 @@ typedef struct {
   void (*write_metric)(void* ctx, int chain, double stepsize, const char* metric_type,
                        const double* inv_metric, int n);
   int want_diagnostics; /* nonzero: the diagnostic writer receives q, p, g rows */
+  int chains_concurrent; /* nonzero: chains' writers may run concurrently */
 } gbnuts_callbacks;
+
+/* Stan CSV files as the sample and diagnostic writers and JSON files as the
+ * metric writer, for num_chains chains with ids chain_id0 + c:
+ * <sample_prefix>_<id>.csv, <diagnostic_prefix>_<id>.csv (when not NULL; sets
+ * want_diagnostics) and <metric_prefix>_<id>.json (when not NULL).  Rows are
+ * stream_writer rows (stream_writer.hpp:16-103: comma-separated, values at
+ * sig_figs significant digits as operator<< prints them, "# " before
+ * messages); the metric file is json_writer's record (json_writer.hpp,
+ * base_hmc.hpp:70-76).  Fills cb (log and interrupt NULL, chains_concurrent
+ * set); gbnuts_csv_close flushes and closes every file and reports a failed
+ * write.  NOINPUT when a file cannot be created. */
+typedef struct gbnuts_csv gbnuts_csv;
+int gbnuts_csv_open(const char* sample_prefix, const char* diagnostic_prefix,
+                    const char* metric_prefix, int num_chains, int chain_id0, int sig_figs,
+                    gbnuts_callbacks* cb, gbnuts_csv** out);
+int gbnuts_csv_close(gbnuts_csv* w);
 
 /* hmc_nuts_diag_e_adapt, multi-chain (hmc_nuts_diag_e_adapt.hpp:331-343
  * argument order).  inits: num_chains x D unconstrained values, or NULL for
@@ -253,6 +274,17 @@ enum {
 
 int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* cfg,
                       gbnuts_run_output* out, const gbnuts_callbacks* cb);
+
+/* Writes a finished run (cfg and out of gbnuts_sample_run) through the writer
+ * callbacks exactly as the service functions do (mcmc_writer.hpp:63-259): per
+ * chain the init writer's values, the sample and diagnostic names, warmup
+ * rows, "Adaptation terminated" with the step size and inverse metric (and the
+ * metric record), sampling rows and the timing block.  The diagnostic writer
+ * receives rows only when cb->want_diagnostics is set and out->diagnostics was
+ * filled.  With gbnuts_csv_open's callbacks this writes Stan CSV files after a
+ * run of the array API or the pool. */
+int gbnuts_write_run(const gbnuts_model* m, const gbnuts_run_config* cfg,
+                     const gbnuts_run_output* out, const gbnuts_callbacks* cb);
 
 /* ------------------------------------------------------------ fit pool */
 

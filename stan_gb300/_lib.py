@@ -37,7 +37,8 @@ class Callbacks(ctypes.Structure):
     _fields_ = [("ctx", ctypes.c_void_p), ("write_names", WRITE_NAMES),
                 ("write_values", WRITE_VALUES), ("write_message", WRITE_MESSAGE),
                 ("write_blank", WRITE_BLANK), ("log", LOG), ("interrupt", INTERRUPT),
-                ("write_metric", WRITE_METRIC), ("want_diagnostics", ctypes.c_int)]
+                ("write_metric", WRITE_METRIC), ("want_diagnostics", ctypes.c_int),
+                ("chains_concurrent", ctypes.c_int)]
 
 
 class RunConfig(ctypes.Structure):
@@ -124,6 +125,13 @@ SIGNATURES = {
     "gbnuts_summary": (ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       _dp]),
+    "gbnuts_write_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RunConfig),
+                                        ctypes.POINTER(RunOutput), ctypes.POINTER(Callbacks)]),
+    "gbnuts_csv_open": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(Callbacks),
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    "gbnuts_csv_close": (ctypes.c_int, [ctypes.c_void_p]),
     "gbnuts_device_info": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "gbnuts_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
 }

@@ -14,7 +14,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgbnuts.so")
-SOURCES = ["loglik.cu", "nuts.cu", "capi.cu", "glm_tc.cu", "noalloc.cu", "pool.cu", "glm_tct.cu", "glm_gemm.cu", "ess.cu"]
+SOURCES = ["loglik.cu", "nuts.cu", "capi.cu", "glm_tc.cu", "noalloc.cu", "pool.cu", "glm_tct.cu",
+           "glm_gemm.cu", "ess.cu", "csv.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -48,7 +49,7 @@ def build(verbose=False, force=False):
         flags += ["-Xptxas", "-v"]
 
     def compile_one(src):
-        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         cmd = [nvcc()] + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -60,7 +61,7 @@ def build(verbose=False, force=False):
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcublas", "-lcudart"]
+    cmd = [nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcublas", "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

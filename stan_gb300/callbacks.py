@@ -116,3 +116,39 @@ class StructuredWriter:
 
     def end_record(self):
         pass
+
+
+class CsvFiles:
+    """Native Stan CSV output (gbnuts_csv_open): per chain <sample_prefix>_<id>.csv,
+    optionally <diagnostic_prefix>_<id>.csv and the metric record
+    <metric_prefix>_<id>.json, ids from the service's init_chain_id.  The
+    service formats rows in native code, chains in parallel; pass it as
+    `csv=` to the service functions (their Python writer arguments are then
+    unused; logger and interrupt still apply)."""
+
+    def __init__(self, sample_prefix, diagnostic_prefix=None, metric_prefix=None, sig_figs=6):
+        self.sample_prefix = sample_prefix
+        self.diagnostic_prefix = diagnostic_prefix
+        self.metric_prefix = metric_prefix
+        self.sig_figs = sig_figs
+        self._h = None
+
+    def open(self, num_chains, chain_id0):
+        import ctypes
+
+        from . import _lib
+        cb = _lib.Callbacks()
+        h = ctypes.c_void_p()
+        enc = (lambda s: None if s is None else str(s).encode())
+        rc = _lib.load().gbnuts_csv_open(enc(self.sample_prefix), enc(self.diagnostic_prefix),
+                                         enc(self.metric_prefix), num_chains, chain_id0,
+                                         self.sig_figs, ctypes.byref(cb), ctypes.byref(h))
+        _lib.check(rc, "gbnuts_csv_open")
+        self._h = h
+        return cb
+
+    def close(self):
+        from . import _lib
+        if self._h is not None:
+            h, self._h = self._h, None
+            _lib.check(_lib.load().gbnuts_csv_close(h), "gbnuts_csv_close")

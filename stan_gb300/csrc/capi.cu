@@ -18,6 +18,8 @@
 #include <sstream>
 #include <string>
 #include <vector>
+#include <thread>
+#include <atomic>
 
 #include "../../include/gbnuts.h"
 #include "gbnuts_internal.h"
@@ -823,6 +825,9 @@ void write_timing(const gbnuts_callbacks* cb, int c, int w, double warm, double 
   emit_blank(cb, c, w);
 }
 
+int write_run(const gbnuts_model* m, const gbnuts_run_config& rc, const gbnuts_run_output& o,
+              const gbnuts_callbacks* cb);
+
 int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* cb) {
   const int C = rc.num_chains, D = m ? m->desc.D : 0;
   if (!m || C <= 0) return fail(GBNUTS_USAGE, "bad arguments");
@@ -871,6 +876,24 @@ int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* c
       return GBNUTS_CONFIG;
     }
   }
+  return write_run(m, rc, o, cb);
+}
+
+// Writes a finished run through the writer callbacks in the service protocol
+// (mcmc_writer.hpp:63-259, run_adaptive_sampler.hpp:46-103): per chain the
+// init values, the names, warmup rows, the adaptation block, sampling rows and
+// the timing block, with the reference's messages for failed chains.
+int write_run(const gbnuts_model* m, const gbnuts_run_config& rc, const gbnuts_run_output& o,
+              const gbnuts_callbacks* cb) {
+  const int C = rc.num_chains, D = m->desc.D, n_cols = 7 + D;
+  const bool diag = cb && cb->want_diagnostics && o.diagnostics;
+  const int* status = o.status;
+  const int* n_rows = o.n_rows;
+  const int* n_warm = o.n_warmup_rows;
+  const double* eps = o.stepsize;
+  const double* invm = o.inv_metric;
+  const double* init = o.init;
+  const double* secs = o.seconds;
   std::vector<std::string> cnames, unames;
   host_names(m->desc, true, cnames);
   host_names(m->desc, false, unames);
@@ -882,25 +905,26 @@ int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* c
   for (auto& s : unames) dnames.push_back(s);
   for (auto& s : unames) dnames.push_back("p_" + s);
   for (auto& s : unames) dnames.push_back("g_" + s);
-  int code = GBNUTS_OK;
-  std::vector<double> drow(7 + 3 * D);
-  for (int c = 0; c < C; ++c) {
-    emit_values(cb, c, GBNUTS_INIT_WRITER, init.data() + (size_t)c * D, D);
+  // one chain's rows and messages, in the reference's order; chains touch
+  // only their own writers
+  auto emit_chain = [&](int c) -> int {
+    std::vector<double> drow(7 + 3 * D);
+    emit_values(cb, c, GBNUTS_INIT_WRITER, init + (size_t)c * D, D);
     if (status[c] == GBNUTS_CHAIN_STEPSIZE_INIT_FAILED) {
       // run_adaptive_sampler.hpp:61-68
       emit_log(cb, GBNUTS_ERROR, "Exception initializing step size.");
       emit_log(cb, GBNUTS_ERROR, "Posterior is improper. Please check your model.");
-      continue;
+      return GBNUTS_OK;
     }
     emit_names(cb, c, GBNUTS_SAMPLE_WRITER, snames);
     emit_names(cb, c, GBNUTS_DIAGNOSTIC_WRITER, dnames);
-    const double* base = draws.data() + (size_t)c * o.max_rows * n_cols;
+    const double* base = o.draws + (size_t)c * o.max_rows * n_cols;
     auto write_rows = [&](int from, int to) {
       for (int i = from; i < to; ++i) {
         emit_values(cb, c, GBNUTS_SAMPLE_WRITER, base + (size_t)i * n_cols, n_cols);
         if (diag) {
           memcpy(drow.data(), base + (size_t)i * n_cols, 7 * sizeof(double));
-          memcpy(drow.data() + 7, dg.data() + ((size_t)c * o.max_rows + i) * 3 * D,
+          memcpy(drow.data() + 7, o.diagnostics + ((size_t)c * o.max_rows + i) * 3 * D,
                  3 * D * sizeof(double));
           emit_values(cb, c, GBNUTS_DIAGNOSTIC_WRITER, drow.data(), 7 + 3 * D);
         }
@@ -917,7 +941,7 @@ int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* c
       for (int d = 0; d < D; ++d) s << (d ? ", " : "") << invm[(size_t)c * D + d];
       emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, s.str());
       if (rc.adapt && cb && cb->write_metric)
-        cb->write_metric(cb->ctx, c, eps[c], "diag_e", invm.data() + (size_t)c * D, D);
+        cb->write_metric(cb->ctx, c, eps[c], "diag_e", invm + (size_t)c * D, D);
     }
     write_rows(n_warm[c], n_rows[c]);
     if (status[c] == GBNUTS_CHAIN_OK) {
@@ -944,9 +968,34 @@ int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* c
         emit_log(cb, GBNUTS_ERROR, "Posterior is improper. Please check your model.");
       else
         emit_log(cb, GBNUTS_ERROR, "Sampling interrupted.");
-      code = GBNUTS_SOFTWARE;
+      return GBNUTS_SOFTWARE;
     }
+    return GBNUTS_OK;
+  };
+  std::vector<int> codes(C, GBNUTS_OK);
+  const int nt = (cb && cb->chains_concurrent)
+                     ? std::min(C, std::max(1, (int)std::thread::hardware_concurrency()))
+                     : 1;
+  if (nt > 1) {
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t)
+      pool.emplace_back([&] {
+        for (int c; (c = next.fetch_add(1)) < C;) {
+          try {
+            codes[c] = emit_chain(c);
+          } catch (...) {
+            codes[c] = GBNUTS_SOFTWARE;
+          }
+        }
+      });
+    for (auto& t : pool) t.join();
+  } else {
+    for (int c = 0; c < C; ++c) codes[c] = emit_chain(c);
   }
+  int code = GBNUTS_OK;
+  for (int c = 0; c < C; ++c)
+    if (codes[c] != GBNUTS_OK) code = codes[c];
   return code;
 }
 
@@ -1013,4 +1062,27 @@ extern "C" int gbnuts_hmc_nuts_diag_e(gbnuts_model* m, int num_chains, const dou
   rc.inits = inits;
   rc.inv_metrics = inv_metrics;
   return run_service(m, rc, cb);
+}
+
+extern "C" int gbnuts_write_run(const gbnuts_model* m, const gbnuts_run_config* rc,
+                                const gbnuts_run_output* out, const gbnuts_callbacks* cb) {
+  using namespace gbn;
+  if (!m || !rc || !out || rc->num_chains <= 0 || !out->draws || !out->n_rows ||
+      !out->n_warmup_rows || !out->status || !out->stepsize || !out->inv_metric || !out->init ||
+      !out->seconds || out->n_cols != 7 + m->desc.D || out->max_rows <= 0) {
+    set_last_error("gbnuts_write_run: bad arguments");
+    return GBNUTS_USAGE;
+  }
+  for (int c = 0; c < rc->num_chains; ++c)
+    if (out->n_rows[c] < 0 || out->n_rows[c] > out->max_rows || out->n_warmup_rows[c] < 0 ||
+        out->n_warmup_rows[c] > out->n_rows[c]) {
+      set_last_error("gbnuts_write_run: row counts outside the output");
+      return GBNUTS_USAGE;
+    }
+  try {
+    return write_run(m, *rc, *out, cb);
+  } catch (const std::exception& e) {
+    set_last_error(std::string("gbnuts_write_run: ") + e.what());
+    return GBNUTS_SOFTWARE;
+  }
 }

@@ -91,6 +91,7 @@ def prepare(D, num_chains=4, adapt=True, num_warmup=1000, num_samples=1000, num_
                          _ptr(res.seconds), 0.0, 0.0, 0, 0,
                          None if res.ess is None else _ptr(res.ess),
                          None if res.summary is None else _ptr(res.summary))
+    res._run = (cfg, out)
     return cfg, out, res
 
 
@@ -99,6 +100,20 @@ def finish(out, res):
     res.total_ms, res.grad_ms = out.total_ms, out.grad_ms
     res.steps, res.kernel_launches = out.steps, out.kernel_launches
     return res
+
+
+def write_csv(model, result, csv):
+    """Writes a finished run (a RunResult of run(), or of a pool) as Stan CSV
+    through a callbacks.CsvFiles, in the service functions' protocol
+    (gbnuts_write_run; chains formatted concurrently)."""
+    cfg, out = result._run
+    cb = csv.open(cfg.num_chains, cfg.init_chain_id)
+    try:
+        rc = _lib.load().gbnuts_write_run(model.handle, ctypes.byref(cfg), ctypes.byref(out),
+                                          ctypes.byref(cb))
+    finally:
+        csv.close()
+    _lib.check(rc, "gbnuts_write_run")
 
 
 def run(model, num_chains=4, **kwargs):

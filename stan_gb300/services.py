@@ -103,13 +103,32 @@ class _Bridge:
         self._guard(f)
 
 
+def _callbacks(bridge, csv, num_chains, chain_id0):
+    """The bridge's callbacks, or the native CSV writer's with the bridge's
+    logger and interrupt."""
+    if csv is None:
+        return bridge.cb
+    cb = csv.open(num_chains, chain_id0)
+    cb.log = bridge.cb.log
+    cb.interrupt = bridge.cb.interrupt
+    return cb
+
+
+def _finish(bridge, csv):
+    if csv is not None:
+        csv.close()
+    if bridge.error is not None:
+        raise bridge.error
+
+
 def hmc_nuts_diag_e_adapt(model, num_chains, init, init_inv_metric, random_seed, init_chain_id,
                           init_radius, num_warmup, num_samples, num_thin, save_warmup, refresh,
                           stepsize, stepsize_jitter, max_depth, delta, gamma, kappa, t0,
                           init_buffer, term_buffer, window, interrupt=None, logger=None,
                           init_writer=None, sample_writer=None, diagnostic_writer=None,
-                          metric_writer=None, precision="fp64"):
-    """Adaptive diag_e NUTS for num_chains chains; writers are lists (one per chain)."""
+                          metric_writer=None, precision="fp64", csv=None):
+    """Adaptive diag_e NUTS for num_chains chains; writers are lists (one per chain),
+    or csv: a callbacks.CsvFiles that writes Stan CSV files natively."""
     D = model.D
     bridge = _Bridge(num_chains, logger, interrupt,
                      _as_list(init_writer, num_chains, Writer),
@@ -119,14 +138,14 @@ def hmc_nuts_diag_e_adapt(model, num_chains, init, init_inv_metric, random_seed,
     ini = _context_matrix(init, num_chains, D, "theta")
     imi = _context_matrix(init_inv_metric, num_chains, D, "inv_metric")
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
+    cb = _callbacks(bridge, csv, num_chains, init_chain_id)
     rc = _lib.load().gbnuts_hmc_nuts_diag_e_adapt(
         model.handle, num_chains, None if ini is None else ini.ctypes.data_as(_dp),
         None if imi is None else imi.ctypes.data_as(_dp), random_seed, init_chain_id,
         init_radius, num_warmup, num_samples, num_thin, int(save_warmup), refresh, stepsize,
         stepsize_jitter, max_depth, delta, gamma, kappa, t0, init_buffer, term_buffer, window,
-        prec, ctypes.byref(bridge.cb))
-    if bridge.error is not None:
-        raise bridge.error
+        prec, ctypes.byref(cb))
+    _finish(bridge, csv)
     return rc
 
 
@@ -134,8 +153,9 @@ def hmc_nuts_diag_e(model, num_chains, init, init_inv_metric, random_seed, init_
                     init_radius, num_warmup, num_samples, num_thin, save_warmup, refresh,
                     stepsize, stepsize_jitter, max_depth, interrupt=None, logger=None,
                     init_writer=None, sample_writer=None, diagnostic_writer=None,
-                    precision="fp64"):
-    """Non-adaptive diag_e NUTS (the resume path) for num_chains chains."""
+                    precision="fp64", csv=None):
+    """Non-adaptive diag_e NUTS (the resume path) for num_chains chains (csv as
+    for hmc_nuts_diag_e_adapt)."""
     D = model.D
     bridge = _Bridge(num_chains, logger, interrupt,
                      _as_list(init_writer, num_chains, Writer),
@@ -145,11 +165,11 @@ def hmc_nuts_diag_e(model, num_chains, init, init_inv_metric, random_seed, init_
     ini = _context_matrix(init, num_chains, D, "theta")
     imi = _context_matrix(init_inv_metric, num_chains, D, "inv_metric")
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
+    cb = _callbacks(bridge, csv, num_chains, init_chain_id)
     rc = _lib.load().gbnuts_hmc_nuts_diag_e(
         model.handle, num_chains, None if ini is None else ini.ctypes.data_as(_dp),
         None if imi is None else imi.ctypes.data_as(_dp), random_seed, init_chain_id,
         init_radius, num_warmup, num_samples, num_thin, int(save_warmup), refresh, stepsize,
-        stepsize_jitter, max_depth, prec, ctypes.byref(bridge.cb))
-    if bridge.error is not None:
-        raise bridge.error
+        stepsize_jitter, max_depth, prec, ctypes.byref(cb))
+    _finish(bridge, csv)
     return rc
