@@ -42,7 +42,7 @@ class _SamplerConfig(ctypes.Structure):
         ("kappa", ctypes.c_double), ("t0", ctypes.c_double),
         ("init_buffer", ctypes.c_uint), ("term_buffer", ctypes.c_uint), ("window", ctypes.c_uint),
         ("init_radius", ctypes.c_double), ("seed", ctypes.c_uint), ("init_chain_id", ctypes.c_uint),
-        ("adapt", ctypes.c_int),
+        ("adapt", ctypes.c_int), ("dense", ctypes.c_int),
     ]
 
 
@@ -82,6 +82,10 @@ def lib():
             ctypes.c_int, ctypes.c_int, dp, dp, ctypes.POINTER(ctypes.c_int),
             ctypes.c_char_p, ctypes.c_int]
         L.oracle_mock_scenario.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, ctypes.c_int]
+        L.oracle_covar_adaptation.argtypes = [ctypes.c_uint] * 4 + [
+            ctypes.c_int, ctypes.c_int, dp, dp, ctypes.POINTER(ctypes.c_int)]
+        L.oracle_dense_metric.argtypes = [ctypes.c_int, dp, dp, dp, dp, ctypes.c_uint,
+                                          ctypes.c_uint, ctypes.c_int, dp]
         _lib = L
     return _lib
 
@@ -137,20 +141,21 @@ class OracleModel:
                save_warmup=False, stepsize=1.0, stepsize_jitter=0.0, max_depth=10,
                delta=0.8, gamma=0.05, kappa=0.75, t0=10.0, init_buffer=75, term_buffer=50,
                window=25, init_radius=2.0, seed=0, init_chain_id=1, adapt=True,
-               inits=None, inv_metrics=None, num_threads=None):
-        """Runs hmc_nuts_diag_e_adapt (adapt=True) or hmc_nuts_diag_e on the CPU."""
+               inits=None, inv_metrics=None, num_threads=None, dense=False):
+        """Runs hmc_nuts_diag_e_adapt (adapt=True) or hmc_nuts_diag_e on the CPU;
+        dense=True: the dense_e services (inverse metrics D x D per chain)."""
         D = self.D
         cfg = _SamplerConfig(num_warmup, num_samples, num_thin, int(save_warmup), 0,
                              stepsize, stepsize_jitter, max_depth, delta, gamma, kappa, t0,
                              init_buffer, term_buffer, window, init_radius, seed,
-                             init_chain_id, int(adapt))
+                             init_chain_id, int(adapt), int(dense))
         n_rows = (num_warmup if save_warmup else 0) + num_samples
         n_rows = (n_rows + num_thin - 1) // num_thin + 2
         C = num_chains
         rows = np.zeros((C, n_rows, N_SAMPLER_COLS + D))
         unc = np.zeros((C, n_rows, D))
         init = np.zeros((C, D))
-        im = np.zeros((C, D))
+        im = np.zeros((C, D, D) if dense else (C, D))
         eps = np.zeros(C)
         ng = np.zeros(C, dtype=np.int64)
         ns = np.zeros(C, dtype=np.int32)
@@ -170,7 +175,8 @@ class OracleModel:
                 used[i].ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)),
                 ngt[i:i + 1].ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
         ini = None if inits is None else np.ascontiguousarray(inits, dtype=np.float64).reshape(C, D)
-        imi = None if inv_metrics is None else np.ascontiguousarray(inv_metrics, dtype=np.float64).reshape(C, D)
+        imi = None if inv_metrics is None else np.ascontiguousarray(
+            inv_metrics, dtype=np.float64).reshape((C, D, D) if dense else (C, D))
         nt = num_threads or os.cpu_count() or 1
         lib().oracle_sample(self._h, ctypes.byref(cfg), C, None if ini is None else _dp(ini),
                             None if imi is None else _dp(imi), nt, outs)
@@ -214,6 +220,34 @@ def var_adaptation(num_warmup, init_buffer, term_buffer, window, q, var0):
                                      buf, 8192)
     lines = [l for l in buf.value.decode().split("\n") if l]
     return rc, var, upd, lines
+
+
+def covar_adaptation(num_warmup, init_buffer, term_buffer, window, q, covar0):
+    """covar_adaptation.learn_covariance over the rows of q; returns (rc, covar, updates)."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    n, d = q.shape
+    covar = np.ascontiguousarray(covar0, dtype=np.float64).reshape(d, d).copy()
+    upd = np.zeros(n, dtype=np.int32)
+    rc = lib().oracle_covar_adaptation(num_warmup, init_buffer, term_buffer, window, d, n,
+                                       _dp(q), _dp(covar),
+                                       upd.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return rc, covar, upd
+
+
+def dense_metric(inv_metric, p=None, seed=0, chain=1, n=0):
+    """dense_e_metric at inverse metric a: (T(p), dtau_dp(p), n momenta from
+    sample_p); None when a fails the services' validation."""
+    a = np.ascontiguousarray(inv_metric, dtype=np.float64)
+    d = a.shape[0]
+    T = np.zeros(1)
+    dt = np.zeros(d)
+    pv = None if p is None else np.ascontiguousarray(p, dtype=np.float64)
+    out = np.zeros((max(n, 1), d))
+    rc = lib().oracle_dense_metric(d, _dp(a), None if pv is None else _dp(pv), _dp(T), _dp(dt),
+                                   seed, chain, n, _dp(out))
+    if rc != 0:
+        return None
+    return float(T[0]), dt, out[:n]
 
 
 def mock_scenario(scenario, uniforms=()):

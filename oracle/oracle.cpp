@@ -434,6 +434,78 @@ class DiagEHamiltonian : public Hamiltonian {
   long long n_grad = 0;
 };
 
+// Cholesky factor of the lower triangle of a (row-major n x n): l lower
+// with a = l l^T, column by column, every element's dot product summed in
+// ascending k (the device computes the same sums in the same order).
+// Returns false when a pivot is not positive (not positive definite).
+static bool cholesky_lower(const Vec& a, int n, Vec& l) {
+  l.assign((size_t)n * n, 0.0);
+  bool ok = true;
+  for (int j = 0; j < n; ++j) {
+    Vec s(n, 0.0);
+    for (int i = j; i < n; ++i) {
+      double v = a[(size_t)i * n + j];
+      for (int k = 0; k < j; ++k) v = v - l[(size_t)i * n + k] * l[(size_t)j * n + k];
+      s[i] = v;
+    }
+    if (!(s[j] > 0)) ok = false;
+    const double d = std::sqrt(s[j]);
+    l[(size_t)j * n + j] = d;
+    for (int i = j + 1; i < n; ++i) l[(size_t)i * n + j] = s[i] / d;
+  }
+  return ok;
+}
+
+// dense_e_metric (dense_e_metric.hpp:17-62): T = 1/2 p . (A p), dtau_dp = A p
+// (row i summed over ascending j), sample_p: p = U^{-1} u with A = U^T U,
+// U = L^T (the reference's inv_e_metric_.llt().matrixU().solve(u)), solved
+// column by column from the last: p_j = r_j / U_jj, then r_i -= U_ij p_j.
+class DenseEHamiltonian : public Hamiltonian {
+ public:
+  DenseEHamiltonian(const Model& m, int D) : model_(m), D_(D) {
+    Vec eye((size_t)D * D, 0.0);
+    for (int i = 0; i < D; ++i) eye[(size_t)i * D + i] = 1.0;
+    set_metric(eye);
+  }
+  bool set_metric(const Vec& a) {
+    inv_metric = a;
+    return cholesky_lower(inv_metric, D_, chol);
+  }
+  Vec mul(const Vec& p) const {
+    Vec t(D_);
+    for (int i = 0; i < D_; ++i) {
+      double v = 0.0;
+      for (int j = 0; j < D_; ++j) v = v + inv_metric[(size_t)i * D_ + j] * p[j];
+      t[i] = v;
+    }
+    return t;
+  }
+  double T(PsPoint& z) override { return 0.5 * dot(z.p, mul(z.p)); }
+  Vec dtau_dp(PsPoint& z) override { return mul(z.p); }
+  Vec dphi_dq(PsPoint& z) override { return z.g; }
+  void sample_p(PsPoint& z, DrawSource& rng) override {
+    Vec r(D_);
+    for (int i = 0; i < D_; ++i) r[i] = rng.normal();
+    for (int j = D_ - 1; j >= 0; --j) {
+      const double pj = r[j] / chol[(size_t)j * D_ + j];
+      z.p[j] = pj;
+      for (int i = 0; i < j; ++i) r[i] = r[i] - chol[(size_t)j * D_ + i] * pj;
+    }
+  }
+  void update_potential_gradient(PsPoint& z) override {
+    Vec grad(z.q.size());
+    double lp = model_.eval(z.q.data(), grad.data(), true, true);
+    ++n_grad;
+    z.V = std::isfinite(lp) ? -lp : (std::isnan(lp) ? lp : INF);
+    for (size_t i = 0; i < grad.size(); ++i) z.g[i] = -grad[i];
+  }
+  const Model& model_;
+  int D_;
+  Vec inv_metric;  // row-major D x D
+  Vec chol;        // L, row-major, lower
+  long long n_grad = 0;
+};
+
 // mock_hamiltonian (src/test/unit/mcmc/hmc/mock_hmc.hpp:38-63)
 class MockHamiltonian : public Hamiltonian {
  public:
@@ -888,6 +960,110 @@ class AdaptDiagENuts : public Nuts {
   }
 };
 
+// welford_covar_estimator (Stan Math; used at covar_adaptation.hpp:51):
+// m += delta / n, m2 += (q - m) delta^T, covariance m2 / (n - 1) when n > 1.
+struct WelfordCovar {
+  double n = 0;
+  int d = 0;
+  Vec m, m2;
+  explicit WelfordCovar(int dim = 0) : d(dim), m(dim, 0.0), m2((size_t)dim * dim, 0.0) {}
+  void restart() {
+    n = 0;
+    std::fill(m.begin(), m.end(), 0.0);
+    std::fill(m2.begin(), m2.end(), 0.0);
+  }
+  void add_sample(const Vec& q) {
+    n += 1;
+    Vec delta(d);
+    for (int i = 0; i < d; ++i) {
+      delta[i] = q[i] - m[i];
+      m[i] = m[i] + delta[i] / n;
+    }
+    for (int i = 0; i < d; ++i)
+      for (int j = 0; j < d; ++j)
+        m2[(size_t)i * d + j] = m2[(size_t)i * d + j] + (q[i] - m[i]) * delta[j];
+  }
+  void sample_covariance(Vec& covar) const {
+    if (n > 1)
+      for (size_t k = 0; k < covar.size(); ++k) covar[k] = m2[k] / (n - 1.0);
+  }
+};
+
+// covar_adaptation (covar_adaptation.hpp:12-57)
+struct CovarAdaptation : WindowedAdaptation {
+  WelfordCovar est;
+  explicit CovarAdaptation(int d) : est(d) {}
+  bool learn_covariance(Vec& covar, const Vec& q) {
+    if (adaptation_window()) est.add_sample(q);
+    if (end_adaptation_window()) {
+      compute_next_window();
+      est.sample_covariance(covar);
+      const double n = est.n;
+      const int d = est.d;
+      for (int i = 0; i < d; ++i)
+        for (int j = 0; j < d; ++j) {
+          double& v = covar[(size_t)i * d + j];
+          v = (n / (n + 5.0)) * v + (i == j ? 1e-3 * (5.0 / (n + 5.0)) : 0.0);
+        }
+      for (double v : covar)
+        if (!std::isfinite(v))
+          throw std::runtime_error(
+              "Numerical overflow in metric adaptation. This occurs when the sampler "
+              "encounters extreme values on the unconstrained space; this may happen when "
+              "the posterior density function is too wide or improper. There may be "
+              "problems with your model specification.");
+      est.restart();
+      ++adapt_window_counter;
+      return true;
+    }
+    ++adapt_window_counter;
+    return false;
+  }
+};
+
+// adapt_dense_e_nuts (adapt_dense_e_nuts.hpp:25-48) on top of dense_e_nuts
+class AdaptDenseENuts : public Nuts {
+ public:
+  AdaptDenseENuts(DenseEHamiltonian& h, Integrator& in, DrawSource& r, int D)
+      : Nuts(h, in, r, D), dham(h), var_adapt(D) {}
+  DenseEHamiltonian& dham;
+  StepsizeAdaptation ss_adapt;
+  CovarAdaptation var_adapt;
+  bool adapt_flag = false;
+  Sample adapt_transition(const Sample& init) {
+    Sample s = transition(init);
+    if (adapt_flag) {
+      ss_adapt.learn_stepsize(nom_epsilon, s.accept_stat);
+      Vec covar = dham.inv_metric;
+      bool update = var_adapt.learn_covariance(covar, z.q);
+      if (update) {
+        dham.set_metric(covar);
+        init_stepsize();
+        ss_adapt.set_mu(std::log(10 * nom_epsilon));
+        ss_adapt.restart();
+      }
+    }
+    return s;
+  }
+  void disengage_adaptation() {
+    adapt_flag = false;
+    ss_adapt.complete_adaptation(nom_epsilon);
+  }
+};
+
+// validate_dense_inv_metric (validate_dense_inv_metric.hpp:20-30) through
+// Stan Math's check_pos_definite: finite, symmetric to 1e-8, and a Cholesky
+// factorisation with positive pivots.
+static bool dense_metric_ok(const Vec& a, int n) {
+  for (double v : a)
+    if (!std::isfinite(v)) return false;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < i; ++j)
+      if (std::fabs(a[(size_t)i * n + j] - a[(size_t)j * n + i]) > 1e-8) return false;
+  Vec l;
+  return n == 0 || cholesky_lower(a, n, l);
+}
+
 // ---------------------------------------------------------------- service
 struct SamplerConfig {
   int num_warmup = 1000, num_samples = 1000, num_thin = 1, save_warmup = 0,
@@ -899,6 +1075,7 @@ struct SamplerConfig {
   double init_radius = 2;
   unsigned seed = 0, init_chain_id = 1;
   int adapt = 1;  // 1: hmc_nuts_diag_e_adapt, 0: hmc_nuts_diag_e
+  int dense = 0;  // 1: the dense_e services (hmc_nuts_dense_e_adapt / hmc_nuts_dense_e)
 };
 
 // Per-chain output.  Rows: lp__, accept_stat__, stepsize__, treedepth__,
@@ -986,25 +1163,41 @@ static void emit_row(const Model& m, const Sample& s, Nuts& sampler, ChainOut& o
 
 // One chain of hmc_nuts_diag_e_adapt (hmc_nuts_diag_e_adapt.hpp:57-112) or
 // hmc_nuts_diag_e (hmc_nuts_diag_e.hpp:48-100).
-static void run_chain(const Model& m, const SamplerConfig& cfg, const double* init,
-                      const double* inv_metric, unsigned chain_id, ChainOut& out) {
+// The initial inverse metric: D values (diag_e) or D x D row-major (dense_e),
+// ones / identity when none is given; false when it fails the services'
+// validation (validate_diag_inv_metric.hpp:18-27, validate_dense_inv_metric.hpp).
+static bool set_initial_metric(DiagEHamiltonian& ham, const double* inv_metric, int D) {
+  Vec im(D, 1.0);
+  if (inv_metric)
+    for (int d = 0; d < D; ++d) im[d] = inv_metric[d];
+  for (double v : im)
+    if (!std::isfinite(v) || !(v > 0)) return false;
+  ham.inv_metric = im;
+  return true;
+}
+static bool set_initial_metric(DenseEHamiltonian& ham, const double* inv_metric, int D) {
+  if (!inv_metric) return true;
+  Vec a(inv_metric, inv_metric + (size_t)D * D);
+  if (!dense_metric_ok(a, D)) return false;
+  ham.set_metric(a);
+  return true;
+}
+
+template <class Ham, class Sampler>
+static void run_chain_t(const Model& m, const SamplerConfig& cfg, const double* init,
+                        const double* inv_metric, unsigned chain_id, ChainOut& out) {
   const int D = m.D;
   PhiloxSource rng(cfg.seed, chain_id);
-  DiagEHamiltonian ham(m, D);
+  Ham ham(m, D);
   ExplLeapfrog integ;
-  AdaptDiagENuts sampler(ham, integ, rng, D);
+  Sampler sampler(ham, integ, rng, D);
   Vec unc;
   try {
     unc = initialize(m, init, rng, cfg.init_radius, out.log, out.n_grad);
-    Vec im(D, 1.0);
-    if (inv_metric)
-      for (int d = 0; d < D; ++d) im[d] = inv_metric[d];
-    for (double v : im)
-      if (!std::isfinite(v) || !(v > 0)) {
-        out.log.error("Inverse Euclidean metric not positive definite.");
-        throw std::domain_error("Initialization failure");
-      }
-    ham.inv_metric = im;
+    if (!set_initial_metric(ham, inv_metric, D)) {
+      out.log.error("Inverse Euclidean metric not positive definite.");
+      throw std::domain_error("Initialization failure");
+    }
   } catch (const std::exception& e) {
     out.log.error(e.what());
     out.return_code = 78;
@@ -1066,6 +1259,14 @@ static void run_chain(const Model& m, const SamplerConfig& cfg, const double* in
   out.n_grad_total = ham.n_grad + out.n_grad - sampler.n_stepsize_trials - sampler.total_leapfrogs;
   out.n_uniform = rng.n_uniform;
   out.n_normal = rng.n_normal;
+}
+
+static void run_chain(const Model& m, const SamplerConfig& cfg, const double* init,
+                      const double* inv_metric, unsigned chain_id, ChainOut& out) {
+  if (cfg.dense)
+    run_chain_t<DenseEHamiltonian, AdaptDenseENuts>(m, cfg, init, inv_metric, chain_id, out);
+  else
+    run_chain_t<DiagEHamiltonian, AdaptDiagENuts>(m, cfg, init, inv_metric, chain_id, out);
 }
 
 // ---------------------------------------------------------------- mock tests
@@ -1162,6 +1363,7 @@ typedef struct {
   double init_radius;
   unsigned seed, init_chain_id;
   int adapt;
+  int dense;  // inverse metrics (in and out) D x D row-major per chain
 } oracle_sampler_config;
 
 typedef struct {
@@ -1205,7 +1407,9 @@ int oracle_sample(void* mp, const oracle_sampler_config* c, int num_chains,
   cfg.seed = c->seed;
   cfg.init_chain_id = c->init_chain_id;
   cfg.adapt = c->adapt;
+  cfg.dense = c->dense;
   const int D = m.D;
+  const size_t MD = cfg.dense ? (size_t)D * D : (size_t)D;
   std::atomic<int> next(0);
   auto worker = [&]() {
     for (;;) {
@@ -1213,7 +1417,7 @@ int oracle_sample(void* mp, const oracle_sampler_config* c, int num_chains,
       if (i >= num_chains) break;
       ChainOut o;
       run_chain(m, cfg, inits ? inits + (size_t)i * D : nullptr,
-                inv_metrics ? inv_metrics + (size_t)i * D : nullptr,
+                inv_metrics ? inv_metrics + (size_t)i * MD : nullptr,
                 cfg.init_chain_id + (unsigned)i, o);
       oracle_chain_out& dst = outs[i];
       if (dst.rows && !o.rows.empty())
@@ -1223,7 +1427,7 @@ int oracle_sample(void* mp, const oracle_sampler_config* c, int num_chains,
       if (dst.init && !o.init.empty())
         std::memcpy(dst.init, o.init.data(), D * sizeof(double));
       if (dst.inv_metric && !o.inv_metric.empty())
-        std::memcpy(dst.inv_metric, o.inv_metric.data(), D * sizeof(double));
+        std::memcpy(dst.inv_metric, o.inv_metric.data(), MD * sizeof(double));
       if (dst.stepsize) *dst.stepsize = o.stepsize;
       if (dst.n_grad) *dst.n_grad = o.n_grad;
       if (dst.n_saved) *dst.n_saved = o.n_saved;
@@ -1289,6 +1493,56 @@ int oracle_var_adaptation(unsigned num_warmup, unsigned init_buffer,
   if (log_buf && log_cap > 0) {
     std::strncpy(log_buf, joined.c_str(), log_cap - 1);
     log_buf[log_cap - 1] = 0;
+  }
+  return 0;
+}
+
+// --- covar_adaptation over n_iter draws q (n_iter x d); covar_out (d x d,
+// row-major) holds the starting covariance and receives the result.
+int oracle_covar_adaptation(unsigned num_warmup, unsigned init_buffer, unsigned term_buffer,
+                            unsigned window, int d, int n_iter, const double* q,
+                            double* covar_out, int* out_update) {
+  Logger logger;
+  CovarAdaptation ca(d);
+  ca.set_window_params(num_warmup, init_buffer, term_buffer, window, logger);
+  Vec covar(covar_out, covar_out + (size_t)d * d);
+  try {
+    for (int i = 0; i < n_iter; ++i) {
+      Vec qi(q + (size_t)i * d, q + (size_t)(i + 1) * d);
+      out_update[i] = ca.learn_covariance(covar, qi) ? 1 : 0;
+    }
+  } catch (const std::exception&) {
+    return 1;
+  }
+  std::copy(covar.begin(), covar.end(), covar_out);
+  return 0;
+}
+
+// --- dense_e_metric pieces: T(p) and dtau_dp for inverse metric a (d x d);
+// n momenta drawn by sample_p from chain `chain`'s normals; the validation.
+// Returns 0, or 1 when a is not a valid inverse metric.
+int oracle_dense_metric(int d, const double* a, const double* p, double* T, double* dtau,
+                        unsigned seed, unsigned chain, int n, double* draws) {
+  Vec av(a, a + (size_t)d * d);
+  if (!dense_metric_ok(av, d)) return 1;
+  Model dummy;
+  DenseEHamiltonian h(dummy, d);
+  h.set_metric(av);
+  PsPoint z(d);
+  if (p) {
+    for (int i = 0; i < d; ++i) z.p[i] = p[i];
+    if (T) *T = h.T(z);
+    if (dtau) {
+      Vec t = h.dtau_dp(z);
+      std::copy(t.begin(), t.end(), dtau);
+    }
+  }
+  if (draws && n > 0) {
+    PhiloxSource rng(seed, chain);
+    for (int k = 0; k < n; ++k) {
+      h.sample_p(z, rng);
+      std::copy(z.p.begin(), z.p.end(), draws + (size_t)k * d);
+    }
   }
   return 0;
 }
