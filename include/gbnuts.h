@@ -199,6 +199,31 @@ int gbnuts_hmc_nuts_diag_e_adapt(gbnuts_model* m, int num_chains, const double* 
                                  unsigned window, int precision,
                                  const gbnuts_callbacks* cb);
 
+/* hmc_nuts_dense_e_adapt (hmc_nuts_dense_e_adapt.hpp:57-118 argument order,
+ * multi-chain): the same service with a dense metric adapted from the
+ * draws' covariance; inv_metrics num_chains x D x D row-major (symmetric
+ * positive definite) or NULL for identities.  The adaptation block writes
+ * "Elements of inverse mass matrix:" and one message per row; write_metric
+ * receives metric_type "dense_e" and n = D * D (row-major). */
+int gbnuts_hmc_nuts_dense_e_adapt(gbnuts_model* m, int num_chains, const double* inits,
+                                  const double* inv_metrics, unsigned random_seed,
+                                  unsigned init_chain_id, double init_radius,
+                                  int num_warmup, int num_samples, int num_thin,
+                                  int save_warmup, int refresh, double stepsize,
+                                  double stepsize_jitter, int max_depth, double delta,
+                                  double gamma, double kappa, double t0,
+                                  unsigned init_buffer, unsigned term_buffer,
+                                  unsigned window, int precision,
+                                  const gbnuts_callbacks* cb);
+
+/* hmc_nuts_dense_e (hmc_nuts_dense_e.hpp): dense metric, adaptation off. */
+int gbnuts_hmc_nuts_dense_e(gbnuts_model* m, int num_chains, const double* inits,
+                            const double* inv_metrics, unsigned random_seed,
+                            unsigned init_chain_id, double init_radius, int num_warmup,
+                            int num_samples, int num_thin, int save_warmup, int refresh,
+                            double stepsize, double stepsize_jitter, int max_depth,
+                            int precision, const gbnuts_callbacks* cb);
+
 /* hmc_nuts_diag_e (hmc_nuts_diag_e.hpp:48-60): the same sampler with
  * adaptation off, given step size and inverse metric (the resume path). */
 int gbnuts_hmc_nuts_diag_e(gbnuts_model* m, int num_chains, const double* inits,
@@ -225,8 +250,14 @@ typedef struct {
   int precision;
   int save_diagnostics;   /* also keep unconstrained q, p, g per saved row */
   const double* inits;        /* num_chains x D or NULL */
-  const double* inv_metrics;  /* num_chains x D or NULL */
+  const double* inv_metrics;  /* num_chains x D (diag_e) or x D x D (dense_e), or NULL */
+  int metric;                 /* GBNUTS_METRIC_DIAG or GBNUTS_METRIC_DENSE */
 } gbnuts_run_config;
+
+/* Euclidean metrics: diag_e (diag_e_metric.hpp, var_adaptation.hpp) and
+ * dense_e (dense_e_metric.hpp, covar_adaptation.hpp).  Dense inverse metrics
+ * are row-major D x D per chain, in and out. */
+enum { GBNUTS_METRIC_DIAG = 0, GBNUTS_METRIC_DENSE = 1 };
 
 /* Per-chain results.  Row layout (n_cols = 7 + D): lp__, accept_stat__,
  * stepsize__, treedepth__, n_leapfrog__, divergent__, energy__, then the
@@ -240,7 +271,7 @@ typedef struct {
   int* n_warmup_rows;     /* per chain: of which warmup rows */
   int* status;            /* per chain: GBNUTS_CHAIN_* */
   double* stepsize;       /* per chain: adapted (or given) step size */
-  double* inv_metric;     /* num_chains x D */
+  double* inv_metric;     /* num_chains x D (diag_e) or num_chains x D x D (dense_e) */
   double* init;           /* num_chains x D unconstrained init used */
   long long* n_grad;      /* per chain: gradient evaluations */
   double* seconds;        /* num_chains x 2: warmup, sampling (wall clock) */

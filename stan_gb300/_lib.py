@@ -13,6 +13,7 @@ OK, USAGE, DATAERR, NOINPUT, SOFTWARE, CONFIG = 0, 64, 65, 66, 70, 78
 LOGISTIC, POISSON, HIER_NORMAL, HIER_LOGISTIC = 1, 2, 3, 4
 F64, F32, BF16 = 0, 1, 2
 PREC_FP64, PREC_FP32, PREC_BF16X3, PREC_BF16 = 0, 1, 2, 3
+METRIC_DIAG, METRIC_DENSE = 0, 1
 PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "bf16x3": PREC_BF16X3, "bf16": PREC_BF16}
 INIT_WRITER, SAMPLE_WRITER, DIAGNOSTIC_WRITER = 0, 1, 2
 CHAIN_STATUS = {0: "ok", 1: "init_failed", 2: "stepsize_init_failed", 3: "stepsize_failed",
@@ -52,7 +53,7 @@ class RunConfig(ctypes.Structure):
                 ("window", ctypes.c_uint), ("init_radius", ctypes.c_double),
                 ("random_seed", ctypes.c_uint), ("init_chain_id", ctypes.c_uint),
                 ("precision", ctypes.c_int), ("save_diagnostics", ctypes.c_int),
-                ("inits", _dp), ("inv_metrics", _dp)]
+                ("inits", _dp), ("inv_metrics", _dp), ("metric", ctypes.c_int)]
 
 
 class RunOutput(ctypes.Structure):
@@ -95,7 +96,17 @@ SIGNATURES = {
         ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
         ctypes.c_double, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_int,
         ctypes.POINTER(Callbacks)]),
+    "gbnuts_hmc_nuts_dense_e_adapt": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_uint, ctypes.c_uint, ctypes.c_double,
+        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+        ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+        ctypes.c_double, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_int,
+        ctypes.POINTER(Callbacks)]),
     "gbnuts_hmc_nuts_diag_e": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_uint, ctypes.c_uint, ctypes.c_double,
+        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+        ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Callbacks)]),
+    "gbnuts_hmc_nuts_dense_e": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_uint, ctypes.c_uint, ctypes.c_double,
         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
         ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Callbacks)]),

@@ -437,6 +437,38 @@ struct DeviceRun {
   }
 };
 
+// L (row-major, lower) with a = L L^T from the lower triangle of the
+// row-major n x n matrix a, column by column with every dot product summed in
+// ascending k, as the step kernel factors adapted metrics; false when a pivot
+// is not positive.
+bool host_cholesky(const double* a, int n, std::vector<double>& l) {
+  l.assign((size_t)n * n, 0.0);
+  std::vector<double> s(n);
+  for (int j = 0; j < n; ++j) {
+    for (int i = j; i < n; ++i) {
+      double v = a[(size_t)i * n + j];
+      for (int k = 0; k < j; ++k) v = v - l[(size_t)i * n + k] * l[(size_t)j * n + k];
+      s[i] = v;
+    }
+    if (!(s[j] > 0)) return false;
+    const double d = sqrt(s[j]);
+    l[(size_t)j * n + j] = d;
+    for (int i = j + 1; i < n; ++i) l[(size_t)i * n + j] = s[i] / d;
+  }
+  return true;
+}
+
+// validate_dense_inv_metric (validate_dense_inv_metric.hpp:20-30) through
+// Stan Math's check_pos_definite: finite, symmetric to 1e-8, positive pivots.
+bool dense_metric_ok(const double* a, int n, std::vector<double>& l) {
+  for (size_t k = 0; k < (size_t)n * n; ++k)
+    if (!isfinite(a[k])) return false;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < i; ++j)
+      if (fabs(a[(size_t)i * n + j] - a[(size_t)j * n + i]) > 1e-8) return false;
+  return host_cholesky(a, n, l);
+}
+
 }  // namespace
 
 int make_sampler_cfg(const gbnuts_model* m, const gbnuts_run_config* rc, int max_rows,
@@ -449,9 +481,17 @@ int make_sampler_cfg(const gbnuts_model* m, const gbnuts_run_config* rc, int max
   // base_nuts::set_max_depth ignores non-positive depths (default 5)
   const int max_depth = rc->max_depth > 0 ? rc->max_depth : 5;
   if (max_depth > MAX_TREE_DEPTH) return fail(GBNUTS_USAGE, "max_depth above 16 is not supported");
-  if (rc->inv_metrics) {
+  if (rc->metric != GBNUTS_METRIC_DIAG && rc->metric != GBNUTS_METRIC_DENSE)
+    return fail(GBNUTS_USAGE, "metric must be GBNUTS_METRIC_DIAG or GBNUTS_METRIC_DENSE");
+  if (rc->inv_metrics && rc->metric == GBNUTS_METRIC_DIAG) {
     for (size_t i = 0; i < (size_t)C * D; ++i)
       if (!isfinite(rc->inv_metrics[i]) || !(rc->inv_metrics[i] > 0))
+        return fail(GBNUTS_CONFIG, "Inverse Euclidean metric not positive definite.");
+  }
+  if (rc->inv_metrics && rc->metric == GBNUTS_METRIC_DENSE) {
+    std::vector<double> l;
+    for (int c = 0; c < C; ++c)
+      if (!dense_metric_ok(rc->inv_metrics + (size_t)c * D * D, D, l))
         return fail(GBNUTS_CONFIG, "Inverse Euclidean metric not positive definite.");
   }
   const int n_cols = 7 + D;
@@ -469,6 +509,7 @@ int make_sampler_cfg(const gbnuts_model* m, const gbnuts_run_config* rc, int max
   cfg.max_depth = max_depth;
   cfg.n_slots = SL_STACK + 6 * max_depth;
   cfg.adapt = rc->adapt ? 1 : 0;
+  cfg.dense = rc->metric == GBNUTS_METRIC_DENSE ? 1 : 0;
   cfg.num_warmup = rc->num_warmup;
   cfg.num_samples = rc->num_samples;
   cfg.num_thin = rc->num_thin;
@@ -541,10 +582,36 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
     GBN_CUDA_TRY(cudaMemcpyAsync(d_inits, rc->inits, (size_t)C * D * sizeof(double),
                                  cudaMemcpyHostToDevice, st));
   }
-  if (rc->inv_metrics) {
+  if (rc->inv_metrics && !cfg.dense) {
     GBN_CUDA_TRY(dr.alloc(&d_invm, (size_t)C * D));
     GBN_CUDA_TRY(cudaMemcpyAsync(d_invm, rc->inv_metrics, (size_t)C * D * sizeof(double),
                                  cudaMemcpyHostToDevice, st));
+  }
+  // dense_e: per chain A (the inverse metric), its Cholesky factor L and the
+  // Welford M2, column-major; A and L from the given metric or the identity
+  double* d_dense = nullptr;
+  const size_t DD = (size_t)D * D;
+  if (cfg.dense) {
+    GBN_CUDA_TRY(dr.alloc(&d_dense, (size_t)C * 3 * DD));
+    std::vector<double> h((size_t)2 * DD), l;
+    for (int c = 0; c < C; ++c) {
+      std::fill(h.begin(), h.end(), 0.0);
+      if (rc->inv_metrics) {
+        const double* a = rc->inv_metrics + (size_t)c * DD;
+        host_cholesky(a, D, l);
+        for (int i = 0; i < D; ++i)
+          for (int j = 0; j < D; ++j) {
+            h[(size_t)j * D + i] = a[(size_t)i * D + j];
+            h[DD + (size_t)j * D + i] = l[(size_t)i * D + j];
+          }
+      } else {
+        for (int i = 0; i < D; ++i) h[(size_t)i * D + i] = h[DD + (size_t)i * D + i] = 1.0;
+      }
+      GBN_CUDA_TRY(cudaMemcpy(d_dense + (size_t)c * 3 * DD, h.data(), 2 * DD * sizeof(double),
+                              cudaMemcpyHostToDevice));
+      GBN_CUDA_TRY(cudaMemsetAsync(d_dense + (size_t)c * 3 * DD + 2 * DD, 0,
+                                   DD * sizeof(double), st));
+    }
   }
   GBN_CUDA_TRY(cudaMemsetAsync(d_done, 0, sizeof(int), st));
   GBN_CUDA_TRY(cudaMemsetAsync(d_abort, 0, sizeof(int), st));
@@ -589,6 +656,7 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   h_fit.m = m->desc;
   h_fit.f = FitPtrs{d_states, d_stacks, d_vecs, d_req, pv, d_active, d_draws,
                     d_diag, d_init, d_inits, d_done, d_abort};
+  h_fit.f.dense = d_dense;
   // the tensor-memory gradient kernel reads the request as packed words
   uint32_t* d_reqw = nullptr;
   struct WordsGuard {
@@ -758,7 +826,16 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   if (out->init)
     GBN_CUDA_TRY(cudaMemcpy(out->init, d_init, (size_t)C * D * sizeof(double),
                             cudaMemcpyDeviceToHost));
-  if (out->inv_metric)
+  if (out->inv_metric && cfg.dense) {
+    std::vector<double> h(DD);
+    for (int c = 0; c < C; ++c) {
+      GBN_CUDA_TRY(cudaMemcpy(h.data(), d_dense + (size_t)c * 3 * DD, DD * sizeof(double),
+                              cudaMemcpyDeviceToHost));
+      for (int i = 0; i < D; ++i)
+        for (int j = 0; j < D; ++j)
+          out->inv_metric[(size_t)c * DD + (size_t)i * D + j] = h[(size_t)j * D + i];
+    }
+  } else if (out->inv_metric)
     GBN_CUDA_TRY(cudaMemcpy2D(out->inv_metric, D * sizeof(double),
                               d_vecs + (size_t)SL_INVM * cfg.ld,
                               (size_t)cfg.n_slots * cfg.ld * sizeof(double), D * sizeof(double),
@@ -839,7 +916,8 @@ int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* c
   std::vector<double> draws((size_t)C * std::max(rows, 1) * n_cols), dg;
   if (diag) dg.resize((size_t)C * std::max(rows, 1) * 3 * D);
   std::vector<int> n_rows(C), n_warm(C), status(C);
-  std::vector<double> eps(C), invm((size_t)C * D), init((size_t)C * D), secs(2 * C);
+  std::vector<double> eps(C), invm((size_t)C * D * (rc.metric == GBNUTS_METRIC_DENSE ? D : 1)),
+      init((size_t)C * D), secs(2 * C);
   std::vector<long long> ngrad(C);
   gbnuts_run_output o;
   memset(&o, 0, sizeof(o));
@@ -936,12 +1014,26 @@ int write_run(const gbnuts_model* m, const gbnuts_run_config& rc, const gbnuts_r
       // mcmc_writer::write_adapt_finish + base_hmc::write_sampler_state
       emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Adaptation terminated");
       emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Step size = " + fmt(eps[c]));
-      emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Diagonal elements of inverse mass matrix:");
-      std::ostringstream s;
-      for (int d = 0; d < D; ++d) s << (d ? ", " : "") << invm[(size_t)c * D + d];
-      emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, s.str());
-      if (rc.adapt && cb && cb->write_metric)
-        cb->write_metric(cb->ctx, c, eps[c], "diag_e", invm + (size_t)c * D, D);
+      if (rc.metric == GBNUTS_METRIC_DENSE) {
+        // dense_e_point::write_metric (dense_e_point.hpp:35-48)
+        const double* a = invm + (size_t)c * D * D;
+        emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Elements of inverse mass matrix:");
+        if (D == 0) emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "");
+        for (int i = 0; i < D; ++i) {
+          std::ostringstream s;
+          for (int j = 0; j < D; ++j) s << (j ? ", " : "") << a[(size_t)i * D + j];
+          emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, s.str());
+        }
+        if (rc.adapt && cb && cb->write_metric)
+          cb->write_metric(cb->ctx, c, eps[c], "dense_e", a, D * D);
+      } else {
+        emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Diagonal elements of inverse mass matrix:");
+        std::ostringstream s;
+        for (int d = 0; d < D; ++d) s << (d ? ", " : "") << invm[(size_t)c * D + d];
+        emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, s.str());
+        if (rc.adapt && cb && cb->write_metric)
+          cb->write_metric(cb->ctx, c, eps[c], "diag_e", invm + (size_t)c * D, D);
+      }
     }
     write_rows(n_warm[c], n_rows[c]);
     if (status[c] == GBNUTS_CHAIN_OK) {
@@ -1001,7 +1093,7 @@ int write_run(const gbnuts_model* m, const gbnuts_run_config& rc, const gbnuts_r
 
 }  // namespace
 
-extern "C" int gbnuts_hmc_nuts_diag_e_adapt(
+static int nuts_adapt_service(int metric,
     gbnuts_model* m, int num_chains, const double* inits, const double* inv_metrics,
     unsigned random_seed, unsigned init_chain_id, double init_radius, int num_warmup,
     int num_samples, int num_thin, int save_warmup, int refresh, double stepsize,
@@ -1033,10 +1125,37 @@ extern "C" int gbnuts_hmc_nuts_diag_e_adapt(
   rc.precision = precision;
   rc.inits = inits;
   rc.inv_metrics = inv_metrics;
+  rc.metric = metric;
   return run_service(m, rc, cb);
 }
 
-extern "C" int gbnuts_hmc_nuts_diag_e(gbnuts_model* m, int num_chains, const double* inits,
+extern "C" int gbnuts_hmc_nuts_diag_e_adapt(
+    gbnuts_model* m, int num_chains, const double* inits, const double* inv_metrics,
+    unsigned random_seed, unsigned init_chain_id, double init_radius, int num_warmup,
+    int num_samples, int num_thin, int save_warmup, int refresh, double stepsize,
+    double stepsize_jitter, int max_depth, double delta, double gamma, double kappa, double t0,
+    unsigned init_buffer, unsigned term_buffer, unsigned window, int precision,
+    const gbnuts_callbacks* cb) {
+  return nuts_adapt_service(GBNUTS_METRIC_DIAG, m, num_chains, inits, inv_metrics, random_seed,
+                            init_chain_id, init_radius, num_warmup, num_samples, num_thin,
+                            save_warmup, refresh, stepsize, stepsize_jitter, max_depth, delta,
+                            gamma, kappa, t0, init_buffer, term_buffer, window, precision, cb);
+}
+
+extern "C" int gbnuts_hmc_nuts_dense_e_adapt(
+    gbnuts_model* m, int num_chains, const double* inits, const double* inv_metrics,
+    unsigned random_seed, unsigned init_chain_id, double init_radius, int num_warmup,
+    int num_samples, int num_thin, int save_warmup, int refresh, double stepsize,
+    double stepsize_jitter, int max_depth, double delta, double gamma, double kappa, double t0,
+    unsigned init_buffer, unsigned term_buffer, unsigned window, int precision,
+    const gbnuts_callbacks* cb) {
+  return nuts_adapt_service(GBNUTS_METRIC_DENSE, m, num_chains, inits, inv_metrics, random_seed,
+                            init_chain_id, init_radius, num_warmup, num_samples, num_thin,
+                            save_warmup, refresh, stepsize, stepsize_jitter, max_depth, delta,
+                            gamma, kappa, t0, init_buffer, term_buffer, window, precision, cb);
+}
+
+static int nuts_service(int metric, gbnuts_model* m, int num_chains, const double* inits,
                                       const double* inv_metrics, unsigned random_seed,
                                       unsigned init_chain_id, double init_radius,
                                       int num_warmup, int num_samples, int num_thin,
@@ -1061,7 +1180,32 @@ extern "C" int gbnuts_hmc_nuts_diag_e(gbnuts_model* m, int num_chains, const dou
   rc.precision = precision;
   rc.inits = inits;
   rc.inv_metrics = inv_metrics;
+  rc.metric = metric;
   return run_service(m, rc, cb);
+}
+
+extern "C" int gbnuts_hmc_nuts_diag_e(gbnuts_model* m, int num_chains, const double* inits,
+                                      const double* inv_metrics, unsigned random_seed,
+                                      unsigned init_chain_id, double init_radius,
+                                      int num_warmup, int num_samples, int num_thin,
+                                      int save_warmup, int refresh, double stepsize,
+                                      double stepsize_jitter, int max_depth, int precision,
+                                      const gbnuts_callbacks* cb) {
+  return nuts_service(GBNUTS_METRIC_DIAG, m, num_chains, inits, inv_metrics, random_seed,
+                      init_chain_id, init_radius, num_warmup, num_samples, num_thin, save_warmup,
+                      refresh, stepsize, stepsize_jitter, max_depth, precision, cb);
+}
+
+extern "C" int gbnuts_hmc_nuts_dense_e(gbnuts_model* m, int num_chains, const double* inits,
+                                      const double* inv_metrics, unsigned random_seed,
+                                      unsigned init_chain_id, double init_radius,
+                                      int num_warmup, int num_samples, int num_thin,
+                                      int save_warmup, int refresh, double stepsize,
+                                      double stepsize_jitter, int max_depth, int precision,
+                                      const gbnuts_callbacks* cb) {
+  return nuts_service(GBNUTS_METRIC_DENSE, m, num_chains, inits, inv_metrics, random_seed,
+                      init_chain_id, init_radius, num_warmup, num_samples, num_thin, save_warmup,
+                      refresh, stepsize, stepsize_jitter, max_depth, precision, cb);
 }
 
 extern "C" int gbnuts_write_run(const gbnuts_model* m, const gbnuts_run_config* rc,

@@ -127,12 +127,30 @@ void csv_metric(void* ctx, int chain, double stepsize, const char* metric_type,
   append_json_value(s, stepsize, w->sig_figs);
   s += ",\n  \"metric_type\" : \"";
   s += metric_type;
-  s += "\",\n  \"inv_metric\" : [ ";
-  for (int i = 0; i < n; ++i) {
-    append_json_value(s, inv[i], w->sig_figs);
-    if (i + 1 < n) s += ", ";
+  s += "\",\n  \"inv_metric\" : ";
+  // a vector, or for dense_e (n = D * D, row-major) json_writer's matrix:
+  // the rows as vectors inside one more bracket
+  auto vec = [&](const double* v, int len) {
+    s += "[ ";
+    for (int i = 0; i < len; ++i) {
+      append_json_value(s, v[i], w->sig_figs);
+      if (i + 1 < len) s += ", ";
+    }
+    s += " ]";
+  };
+  if (strcmp(metric_type, "dense_e") == 0) {
+    int d = 0;
+    while ((long long)(d + 1) * (d + 1) <= n) ++d;
+    s += "[ ";
+    for (int r = 0; r < d; ++r) {
+      vec(inv + (size_t)r * d, d);
+      if (r + 1 < d) s += ", ";
+    }
+    s += " ]";
+  } else {
+    vec(inv, n);
   }
-  s += " ]\n}\n";
+  s += "\n}\n";
   const std::string path = w->metric_prefix + "_" + std::to_string(w->chain_id0 + chain) +
                            ".json";
   FILE* f = fopen(path.c_str(), "wb");

@@ -64,6 +64,7 @@ struct Ctx {
   double* vecs;
   int c, tid, nth;  // chain; thread index in the chain's team, team size
   Team tm;
+  double* dm;  // dense_e: the chain's A, L, M2 (column-major D x D each); null for diag_e
   __device__ double* slot(int s) const {
     return vecs + ((size_t)c * cfg.n_slots + s) * cfg.ld;
   }
@@ -78,8 +79,55 @@ struct Stk {
   int* slot;
 };
 
-// T(p) = 1/2 p . (invM p)  (diag_e_metric.hpp:20-22)
+// dense_e: out = A v, row i summed over ascending j (dense_e_metric.hpp:38,
+// dtau_dp = inv_e_metric_ * p).  Every thread reads all of v: the caller
+// synchronises the team after the last write of v.
+static __device__ void metric_apply(const Ctx& x, const double* __restrict__ v,
+                                    double* __restrict__ out) {
+  const int D = x.cfg.D;
+  const double* __restrict__ A = x.dm;
+  for (int i = x.tid; i < D; i += x.nth) {
+    double s = 0.0;
+    for (int j = 0; j < D; ++j) s = DADD(s, DMUL(A[(size_t)j * D + i], v[j]));
+    out[i] = s;
+  }
+}
+
+// dense_e: L with A = L L^T from A's lower triangle, column by column; each
+// element's dot product summed over ascending k (the reference factors with
+// Eigen's llt() where it draws momenta, dense_e_metric.hpp:54-61).
+static __device__ void dense_cholesky(const Ctx& x) {
+  const int D = x.cfg.D;
+  const double* __restrict__ A = x.dm;
+  double* __restrict__ L = x.dm + (size_t)D * D;
+  for (int e = x.tid; e < D * D; e += x.nth)
+    if (e % D < e / D) L[e] = 0.0;  // strict upper part
+  for (int j = 0; j < D; ++j) {
+    x.tm.sync();
+    for (int i = j + x.tid; i < D; i += x.nth) {
+      double v = A[(size_t)j * D + i];
+      for (int k = 0; k < j; ++k) v = DSUB(v, DMUL(L[(size_t)k * D + i], L[(size_t)k * D + j]));
+      L[(size_t)j * D + i] = v;
+    }
+    x.tm.sync();
+    const double d = sqrt(L[(size_t)j * D + j]);
+    x.tm.sync();
+    for (int i = j + x.tid; i < D; i += x.nth)
+      L[(size_t)j * D + i] = i == j ? d : DDIV(L[(size_t)j * D + i], d);
+  }
+  x.tm.sync();
+}
+
+// T(p) = 1/2 p . (invM p)  (diag_e_metric.hpp:20-22, dense_e_metric.hpp:21-23)
 static __device__ double kinetic(const Ctx& x, const double* p) {
+  if (x.dm) {
+    double* t = x.slot(SL_MS0);
+    x.tm.sync();
+    metric_apply(x, p, t);
+    double s = 0.0;
+    for (int i = x.tid; i < x.cfg.D; i += x.nth) s += p[i] * t[i];
+    return 0.5 * x.tm.sum(s);
+  }
   const double* im = x.slot(SL_INVM);
   double s = 0.0;
 #pragma unroll 4
@@ -93,7 +141,29 @@ static __device__ __forceinline__ double draw_uniform(const SamplerCfg& cfg, Cha
 }
 
 // sample_p (diag_e_metric.hpp:44-50): p_i = n_i / sqrt(invM_i), D normals.
+// dense_e (dense_e_metric.hpp:50-61): p = U^{-1} u with A = U^T U, U = L^T,
+// solved column by column from the last: p_j = r_j / U_jj, r_i -= U_ij p_j.
+static __device__ void sample_p_dense(const Ctx& x, ChainState& st, double* p) {
+  const int D = x.cfg.D;
+  const double* __restrict__ L = x.dm + (size_t)D * D;
+  double* r = x.slot(SL_MS3);
+  const unsigned chain = x.cfg.init_chain_id + (unsigned)x.c;
+  x.tm.sync();
+  for (int i = x.tid; i < D; i += x.nth) r[i] = gbds_normal_at(x.cfg.seed, chain, st.nn + i);
+  st.nn += D;
+  for (int j = D - 1; j >= 0; --j) {
+    x.tm.sync();
+    const double pj = DDIV(r[j], L[(size_t)j * D + j]);
+    for (int i = x.tid; i < j; i += x.nth) r[i] = DSUB(r[i], DMUL(L[(size_t)i * D + j], pj));
+    if (x.tid == j % x.nth) p[j] = pj;
+  }
+}
+
 static __device__ void sample_p(const Ctx& x, ChainState& st, double* p) {
+  if (x.dm) {
+    sample_p_dense(x, st, p);
+    return;
+  }
   const double* im = x.slot(SL_INVM);
   const unsigned chain = x.cfg.init_chain_id + (unsigned)x.c;
   for (int i = x.tid; i < x.cfg.D; i += x.nth)
@@ -118,6 +188,18 @@ static __device__ void half_kick(const Ctx& x, double* __restrict__ p,
 static __device__ void drift_and_request(const Ctx& x, double* __restrict__ q,
                                          const double* __restrict__ p, double eps,
                                          double* __restrict__ req) {
+  if (x.dm) {
+    double* t = x.slot(SL_MS0);
+    x.tm.sync();
+    metric_apply(x, p, t);
+    for (int i = x.tid; i < x.cfg.D; i += x.nth) {
+      const double v = DADD(q[i], DMUL(eps, t[i]));
+      q[i] = v;
+      req[i] = v;
+    }
+    x.tm.sync();
+    return;
+  }
   const double* __restrict__ im = x.slot(SL_INVM);
 #pragma unroll 4
   for (int i = x.tid; i < x.cfg.D; i += x.nth) {
@@ -242,6 +324,56 @@ static __device__ int learn_variance(const Ctx& x, ChainState& st) {
   return 0;
 }
 
+// covar_adaptation::learn_covariance (covar_adaptation.hpp:17-52) with
+// Welford's covariance estimator (m += delta / n, M2 += (q - m) delta^T), then
+// the new metric's Cholesky factor; returns 1 on a metric update, -1 on
+// overflow.
+static __device__ int learn_covariance(const Ctx& x, ChainState& st) {
+  const int D = x.cfg.D;
+  const double* q = x.slot(SL_SMP_Q);
+  double* m = x.slot(SL_WM);
+  double* dl = x.slot(SL_MS0);
+  double* A = x.dm;
+  double* M2 = x.dm + 2 * (size_t)D * D;
+  if (adaptation_window(st)) {
+    st.w_n += 1.0;
+    for (int i = x.tid; i < D; i += x.nth) {
+      const double delta = DSUB(q[i], m[i]);
+      m[i] = DADD(m[i], DDIV(delta, st.w_n));
+      dl[i] = delta;
+    }
+    x.tm.sync();
+    for (int e = x.tid; e < D * D; e += x.nth) {
+      const int i = e % D, j = e / D;
+      M2[e] = DADD(M2[e], DMUL(DSUB(q[i], m[i]), dl[j]));
+    }
+    x.tm.sync();
+  }
+  if (end_adaptation_window(st)) {
+    compute_next_window(st);
+    const double n = st.w_n;
+    const double a = n / (n + 5.0);
+    const double b = 1e-3 * (5.0 / (n + 5.0));
+    int bad = 0;
+    for (int e = x.tid; e < D * D; e += x.nth) {
+      double v = A[e];
+      if (n > 1) v = DDIV(M2[e], n - 1.0);
+      v = DADD(DMUL(a, v), (e % D == e / D) ? b : 0.0);
+      A[e] = v;
+      if (!isfinite(v)) bad = 1;
+      M2[e] = 0.0;
+    }
+    for (int i = x.tid; i < D; i += x.nth) m[i] = 0.0;
+    st.w_n = 0.0;
+    st.wa_counter += 1u;
+    if (x.tm.any(bad)) return -1;
+    dense_cholesky(x);
+    return 1;
+  }
+  st.wa_counter += 1u;
+  return 0;
+}
+
 // The vector pass of an inner merge: rho and the edge momentum of level l,
 // its proposal if the final subtree is selected, and the six U-turn dot
 // products (partial per thread).  Pointers of the two subtrees never alias.
@@ -251,16 +383,17 @@ static __device__ __forceinline__ void merge_level_pass(
     const double* __restrict__ CQ, const double* __restrict__ CP, const double* __restrict__ CG,
     const double* __restrict__ CPB, const double* __restrict__ CPE,
     const double* __restrict__ CR, const double* __restrict__ im, bool sel_final,
-    double* dd) {
+    const double* __restrict__ ps, int ld, double* dd) {
   double d1a = 0, d1b = 0, d2a = 0, d2b = 0, d3a = 0, d3b = 0;
 #pragma unroll 2
   for (int i = tid; i < D; i += nth) {
     const double ipb = IPB[i], ipe = IPE[i], ir = IR[i];
     const double cpb = CPB[i], cpe = CPE[i], cr = CR[i];
-    const double psb = DMUL(im[i], ipb);   // p_sharp_beg
-    const double pse = DMUL(im[i], cpe);   // p_sharp_end
-    const double psie = DMUL(im[i], ipe);  // p_sharp_init_end
-    const double psfb = DMUL(im[i], cpb);  // p_sharp_final_beg
+    // p_sharp = invM p: diag inline, dense precomputed into ps (4 vectors, ld apart)
+    const double psb = ps ? ps[i] : DMUL(im[i], ipb);            // p_sharp_beg
+    const double pse = ps ? ps[ld + i] : DMUL(im[i], cpe);       // p_sharp_end
+    const double psie = ps ? ps[2 * ld + i] : DMUL(im[i], ipe);  // p_sharp_init_end
+    const double psfb = ps ? ps[3 * ld + i] : DMUL(im[i], cpb);  // p_sharp_final_beg
     const double rs = DADD(ir, cr);        // rho_init + rho_final
     const double r2 = DADD(ir, cpb);       // rho_init + p_final_beg
     const double r3 = DADD(cr, ipe);       // rho_final + p_init_end
@@ -294,7 +427,8 @@ static __device__ __forceinline__ void merge_top_pass(
     double* __restrict__ SQ, double* __restrict__ SP, double* __restrict__ SG,
     const double* __restrict__ CQ, const double* __restrict__ CP, const double* __restrict__ CG,
     const double* __restrict__ CPB, const double* __restrict__ CPE,
-    const double* __restrict__ CR, const double* __restrict__ im, double* dd) {
+    const double* __restrict__ CR, const double* __restrict__ im,
+    const double* __restrict__ ps, int ld, double* dd) {
   double d1a = 0, d1b = 0, d2a = 0, d2b = 0, d3a = 0, d3b = 0;
 #pragma unroll 2
   for (int i = tid; i < D; i += nth) {
@@ -315,8 +449,10 @@ static __device__ __forceinline__ void merge_top_pass(
       p_ff = PFF[i];
     }
     const double rho = DADD(rho_bck, rho_fwd);
-    const double ps_bb = DMUL(im[i], p_bb), ps_ff = DMUL(im[i], p_ff);
-    const double ps_fb = DMUL(im[i], p_fb), ps_bf = DMUL(im[i], p_bf);
+    const double ps_ff = ps ? ps[i] : DMUL(im[i], p_ff);
+    const double ps_bb = ps ? ps[ld + i] : DMUL(im[i], p_bb);
+    const double ps_fb = ps ? ps[2 * ld + i] : DMUL(im[i], p_fb);
+    const double ps_bf = ps ? ps[3 * ld + i] : DMUL(im[i], p_bf);
     const double r2 = DADD(rho_bck, p_fb);
     const double r3 = DADD(rho_fwd, p_bf);
     d1a += ps_ff * rho;
@@ -386,9 +522,21 @@ static __device__ bool merge_into_level(const Ctx& x, ChainState& st, const Stk&
     double accept_prob = exp(cur_lsw - lsw_sub);
     sel_final = draw_uniform(cfg, st, x.c) < accept_prob;
   }
+  const double* ps = nullptr;
+  if (x.dm) {
+    // dense p_sharp of the four edge momenta, before the pass overwrites them
+    double* s0 = x.slot(SL_MS0);
+    x.tm.sync();
+    metric_apply(x, IPB, s0);
+    metric_apply(x, CPE, s0 + cfg.ld);
+    metric_apply(x, IPE, s0 + 2 * cfg.ld);
+    metric_apply(x, CPB, s0 + 3 * cfg.ld);
+    x.tm.sync();
+    ps = s0;
+  }
   double dd[6];
   merge_level_pass(cfg.D, x.tid, x.nth, IQ, IP, IG, IPB, IPE, IR, CQ, CP, CG, CPB, CPE, CR,
-                   x.slot(SL_INVM), sel_final, dd);
+                   x.slot(SL_INVM), sel_final, ps, cfg.ld, dd);
   x.tm.sum6(dd);
   const double d1a = dd[0], d1b = dd[1], d2a = dd[2], d2b = dd[3], d3a = dd[4], d3b = dd[5];
   x.tm.sync();
@@ -438,9 +586,21 @@ static __device__ bool merge_top(const Ctx& x, ChainState& st, const Stk& sk, in
   double* SG = x.slot(SL_SMP_G);
   const double* im = x.slot(SL_INVM);
   const bool fwd = st.dir > 0;
+  const double* ps = nullptr;
+  if (x.dm) {
+    // dense p_sharp of p_ff, p_bb, p_fb, p_bf as the pass will select them
+    double* s0 = x.slot(SL_MS0);
+    x.tm.sync();
+    metric_apply(x, fwd ? CPE : PFF, s0);
+    metric_apply(x, fwd ? PBB : CPE, s0 + cfg.ld);
+    metric_apply(x, fwd ? CPB : PBB, s0 + 2 * cfg.ld);
+    metric_apply(x, fwd ? PFF : CPB, s0 + 3 * cfg.ld);
+    x.tm.sync();
+    ps = s0;
+  }
   double dd[6];
   merge_top_pass(cfg.D, x.tid, x.nth, fwd, sel, RHO, PFF, PFB, PBF, PBB, SQ, SP, SG, CQ, CP, CG, CPB,
-                 CPE, CR, im, dd);
+                 CPE, CR, im, ps, cfg.ld, dd);
   if (sel) st.V_smp = cur_V;
   x.tm.sum6(dd);
   const double d1a = dd[0], d1b = dd[1], d2a = dd[2], d2b = dd[3], d3a = dd[4], d3b = dd[5];
@@ -487,7 +647,8 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
   }
   tm.sync();
   const Stk sk{lsw_s, V_s, slot_s};
-  Ctx x{cfg, vecs, c, tid, nth, tm};
+  Ctx x{cfg, vecs, c, tid, nth, tm,
+        f.dense ? f.dense + (size_t)c * 3 * cfg.D * cfg.D : nullptr};
   const int D = cfg.D;
   double* rq = req + (size_t)c * cfg.ld;
   const double inf = __longlong_as_double(0x7ff0000000000000LL);
@@ -849,7 +1010,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         if (st.adapt_flag) {
           learn_stepsize(cfg, st, st.accept);
           tm.sync();
-          const int upd = learn_variance(x, st);
+          const int upd = x.dm ? learn_covariance(x, st) : learn_variance(x, st);
           if (upd < 0) {
             finish_chain(st, GBNUTS_CHAIN_METRIC_OVERFLOW, done_count, tid);
             break;

@@ -13,15 +13,17 @@ constexpr int MAX_TREE_DEPTH = 16;
 // Vector slots of a chain (each `ld` doubles): the two trajectory ends (the
 // end being extended is integrated in place), the current sample, the momenta
 // at the inner and outer edge of the forward and backward halves, the summed
-// momentum, the inverse metric, the Welford accumulators, then 6 slots per
-// stack level (proposal q, p, g; momentum at the subtree's first and last
-// leaf; summed momentum).
+// momentum, the inverse metric, the Welford accumulators, four scratch
+// vectors of the dense metric (A p products), then 6 slots per stack level
+// (proposal q, p, g; momentum at the subtree's first and last leaf; summed
+// momentum).
 enum Slot {
   SL_FWD_Q = 0, SL_FWD_P, SL_FWD_G,
   SL_BCK_Q, SL_BCK_P, SL_BCK_G,
   SL_SMP_Q, SL_SMP_P, SL_SMP_G,
   SL_PFF, SL_PFB, SL_PBF, SL_PBB,
   SL_RHO, SL_INVM, SL_WM, SL_WM2,
+  SL_MS0, SL_MS1, SL_MS2, SL_MS3,
   SL_STACK
 };
 
@@ -42,6 +44,7 @@ struct SamplerCfg {
   unsigned wa_size0, wa_next0;  // window size and end after set_window_params
   unsigned seed, init_chain_id;
   int idx_tau, idx_sigma;
+  int dense;  // 1: dense_e metric (FitPtrs::dense), 0: diag_e (slot SL_INVM)
 };
 
 struct ChainState {
@@ -93,6 +96,10 @@ struct FitPtrs {
   // the request also as chains-on-M tensor-core words (kThetaWords per chain),
   // or null when the gradient form does not read them
   uint32_t* req_tc;
+  // dense_e: per chain three D x D matrices, column-major (element (i, j) at
+  // j * D + i): the inverse metric A, its Cholesky factor L (lower, A = L L^T)
+  // and the Welford second-moment sums M2; null for diag_e
+  double* dense;
 };
 
 void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* stacks,

@@ -443,6 +443,8 @@ int gbnuts_pool_submit(gbnuts_pool* p, int kind, const void* X, int x_dtype, con
   if (rc->num_chains <= 0 || rc->num_chains > p->max_chains)
     return fail(GBNUTS_USAGE, "num_chains must be in 1..max_chains");
   if (!out->draws || !out->n_rows) return fail(GBNUTS_USAGE, "draws / n_rows buffers missing");
+  if (rc->metric != GBNUTS_METRIC_DIAG)
+    return fail(GBNUTS_USAGE, "the pool runs diag_e fits (dense_e runs through gbnuts_sample_run)");
   PendingFit pf;
   pf.id = p->next_id++;
   pf.kind = kind;

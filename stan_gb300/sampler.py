@@ -48,11 +48,13 @@ def prepare(D, num_chains=4, adapt=True, num_warmup=1000, num_samples=1000, num_
             gamma=0.05, kappa=0.75, t0=10.0, init_buffer=75, term_buffer=50, window=25,
             init_radius=2.0, random_seed=0, init_chain_id=1, precision="fp64",
             inits=None, inv_metrics=None, save_diagnostics=False, report_ess=False,
-            report_summary=False):
+            report_summary=False, metric="diag"):
     """Run configuration and caller-owned output buffers for a fit of dimension D.
 
     report_ess: also compute the split rank-normalised bulk / tail ESS of every
     quantity on the device when the fit ends (RunResult.ess).
+    metric: "diag" (diag_e) or "dense" (dense_e; inv_metrics and
+    RunResult.inv_metric are then (chains, D, D)).
     report_summary: also the full convergence summary (ESS, R-hat, MCSE) of every
     quantity, on the device (RunResult.summary; SUMMARY_COLUMNS).
 
@@ -62,19 +64,23 @@ def prepare(D, num_chains=4, adapt=True, num_warmup=1000, num_samples=1000, num_
     C = num_chains
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
     ini = None if inits is None else np.ascontiguousarray(inits, dtype=np.float64).reshape(C, D)
-    imi = None if inv_metrics is None else np.ascontiguousarray(inv_metrics, dtype=np.float64).reshape(C, D)
+    dense = metric == "dense"
+    mshape = (C, D, D) if dense else (C, D)
+    imi = None if inv_metrics is None else np.ascontiguousarray(
+        inv_metrics, dtype=np.float64).reshape(mshape)
     cfg = _lib.RunConfig(C, int(adapt), num_warmup, num_samples, num_thin, int(save_warmup),
                          stepsize, stepsize_jitter, max_depth, delta, gamma, kappa, t0,
                          init_buffer, term_buffer, window, init_radius, random_seed,
                          init_chain_id, prec, int(save_diagnostics),
-                         None if ini is None else _ptr(ini), None if imi is None else _ptr(imi))
+                         None if ini is None else _ptr(ini), None if imi is None else _ptr(imi),
+                         _lib.METRIC_DENSE if dense else _lib.METRIC_DIAG)
     rows = ((num_warmup + num_thin - 1) // num_thin if save_warmup else 0) + \
         (num_samples + num_thin - 1) // num_thin
     rows = max(rows, 1)
     ncol = 7 + D
     res = RunResult(np.zeros((C, rows, ncol)), np.zeros(C, dtype=np.int32),
                     np.zeros(C, dtype=np.int32), np.zeros(C, dtype=np.int32), np.zeros(C),
-                    np.zeros((C, D)), np.zeros((C, D)), np.zeros(C, dtype=np.int64),
+                    np.zeros(mshape), np.zeros((C, D)), np.zeros(C, dtype=np.int64),
                     np.zeros((C, 2)), 0.0, 0.0, 0, 0,
                     np.zeros((C, rows, 3 * D)) if save_diagnostics else None)
     if report_ess:

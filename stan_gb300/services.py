@@ -23,9 +23,9 @@ def _as_list(w, n, factory):
     return [w] * n
 
 
-def _context_matrix(values, num_chains, D, key):
-    """init / init_inv_metric contexts: None, one vector for all chains, a
-    (chains, D) array, or a list of dicts holding `key`."""
+def _context_matrix(values, num_chains, D, key, dense=False):
+    """init / init_inv_metric contexts: None, one vector (one D x D matrix when
+    dense) for all chains, a per-chain array, or a list of dicts holding `key`."""
     if values is None:
         return None
     if isinstance(values, (list, tuple)) and len(values) and isinstance(values[0], dict):
@@ -33,6 +33,10 @@ def _context_matrix(values, num_chains, D, key):
             return None
         values = [v[key] for v in values]
     a = np.asarray(values, dtype=np.float64)
+    if dense:
+        if a.ndim == 2:
+            a = np.tile(a, (num_chains, 1, 1))
+        return np.ascontiguousarray(a.reshape(num_chains, D, D))
     if a.ndim == 1:
         a = np.tile(a, (num_chains, 1))
     return np.ascontiguousarray(a.reshape(num_chains, D))
@@ -98,7 +102,11 @@ class _Bridge:
             w.begin_record()
             w.write("stepsize", stepsize)
             w.write("metric_type", metric_type.decode())
-            w.write("inv_metric", [inv[i] for i in range(n)])
+            vals = [inv[i] for i in range(n)]
+            if metric_type == b"dense_e":  # n = D * D, row-major
+                d = int(round(n ** 0.5))
+                vals = [vals[i * d:(i + 1) * d] for i in range(d)]
+            w.write("inv_metric", vals)
             w.end_record()
         self._guard(f)
 
@@ -126,7 +134,8 @@ def hmc_nuts_diag_e_adapt(model, num_chains, init, init_inv_metric, random_seed,
                           stepsize, stepsize_jitter, max_depth, delta, gamma, kappa, t0,
                           init_buffer, term_buffer, window, interrupt=None, logger=None,
                           init_writer=None, sample_writer=None, diagnostic_writer=None,
-                          metric_writer=None, precision="fp64", csv=None):
+                          metric_writer=None, precision="fp64", csv=None,
+                          _metric=0):
     """Adaptive diag_e NUTS for num_chains chains; writers are lists (one per chain),
     or csv: a callbacks.CsvFiles that writes Stan CSV files natively."""
     D = model.D
@@ -136,10 +145,12 @@ def hmc_nuts_diag_e_adapt(model, num_chains, init, init_inv_metric, random_seed,
                      _as_list(diagnostic_writer, num_chains, Writer),
                      _as_list(metric_writer, num_chains, StructuredWriter))
     ini = _context_matrix(init, num_chains, D, "theta")
-    imi = _context_matrix(init_inv_metric, num_chains, D, "inv_metric")
+    imi = _context_matrix(init_inv_metric, num_chains, D, "inv_metric",
+                          dense=_metric == _lib.METRIC_DENSE)
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
     cb = _callbacks(bridge, csv, num_chains, init_chain_id)
-    rc = _lib.load().gbnuts_hmc_nuts_diag_e_adapt(
+    fn = "gbnuts_hmc_nuts_dense_e_adapt" if _metric else "gbnuts_hmc_nuts_diag_e_adapt"
+    rc = getattr(_lib.load(), fn)(
         model.handle, num_chains, None if ini is None else ini.ctypes.data_as(_dp),
         None if imi is None else imi.ctypes.data_as(_dp), random_seed, init_chain_id,
         init_radius, num_warmup, num_samples, num_thin, int(save_warmup), refresh, stepsize,
@@ -153,7 +164,7 @@ def hmc_nuts_diag_e(model, num_chains, init, init_inv_metric, random_seed, init_
                     init_radius, num_warmup, num_samples, num_thin, save_warmup, refresh,
                     stepsize, stepsize_jitter, max_depth, interrupt=None, logger=None,
                     init_writer=None, sample_writer=None, diagnostic_writer=None,
-                    precision="fp64", csv=None):
+                    precision="fp64", csv=None, _metric=0):
     """Non-adaptive diag_e NUTS (the resume path) for num_chains chains (csv as
     for hmc_nuts_diag_e_adapt)."""
     D = model.D
@@ -163,13 +174,33 @@ def hmc_nuts_diag_e(model, num_chains, init, init_inv_metric, random_seed, init_
                      _as_list(diagnostic_writer, num_chains, Writer),
                      [StructuredWriter() for _ in range(num_chains)])
     ini = _context_matrix(init, num_chains, D, "theta")
-    imi = _context_matrix(init_inv_metric, num_chains, D, "inv_metric")
+    imi = _context_matrix(init_inv_metric, num_chains, D, "inv_metric",
+                          dense=_metric == _lib.METRIC_DENSE)
     prec = _lib.PRECISIONS[precision] if isinstance(precision, str) else precision
     cb = _callbacks(bridge, csv, num_chains, init_chain_id)
-    rc = _lib.load().gbnuts_hmc_nuts_diag_e(
+    fn = "gbnuts_hmc_nuts_dense_e" if _metric else "gbnuts_hmc_nuts_diag_e"
+    rc = getattr(_lib.load(), fn)(
         model.handle, num_chains, None if ini is None else ini.ctypes.data_as(_dp),
         None if imi is None else imi.ctypes.data_as(_dp), random_seed, init_chain_id,
         init_radius, num_warmup, num_samples, num_thin, int(save_warmup), refresh, stepsize,
         stepsize_jitter, max_depth, prec, ctypes.byref(cb))
     _finish(bridge, csv)
     return rc
+
+
+def _dense(fn, name):
+    """The dense_e form of a diag_e service wrapper: same arguments, with
+    init_inv_metric as D x D matrices (one for all chains or one per chain)."""
+    import functools
+
+    @functools.wraps(fn)
+    def wrapper(*args, **kwargs):
+        return fn(*args, _metric=_lib.METRIC_DENSE, **kwargs)
+    wrapper.__name__ = name
+    wrapper.__doc__ = fn.__doc__.replace("diag_e", "dense_e") + (
+        "  Dense form: init_inv_metric D x D.")
+    return wrapper
+
+
+hmc_nuts_dense_e_adapt = _dense(hmc_nuts_diag_e_adapt, "hmc_nuts_dense_e_adapt")
+hmc_nuts_dense_e = _dense(hmc_nuts_diag_e, "hmc_nuts_dense_e")

@@ -135,3 +135,14 @@ def test_open_errors(tmp_path):
                                ctypes.byref(cb), ctypes.byref(h)) == _lib.USAGE
     assert lib.gbnuts_csv_open(str(tmp_path / "x").encode(), None, None, 1, 1, 0,
                                ctypes.byref(cb), ctypes.byref(h)) == _lib.USAGE
+
+
+def test_dense_metric_record_matches_json_writer(tmp_path):
+    # json_writer's Eigen matrix: "[ " rows as "[ a, b ]" joined by ", " " ]"
+    lib, cb, h = _open(tmp_path, chains=1)
+    inv = np.array([1.0, 0.5, 0.5, 2.0])
+    cb.write_metric(cb.ctx, 0, 0.5, b"dense_e", inv.ctypes.data_as(_dp), inv.size)
+    assert lib.gbnuts_csv_close(h) == 0
+    got = (tmp_path / "metric_1.json").read_text()
+    assert got == ('\n{\n  "stepsize" : 0.5,\n  "metric_type" : "dense_e",\n'
+                   '  "inv_metric" : [ [ 1, 0.5 ], [ 0.5, 2 ] ]\n}\n')
