@@ -546,7 +546,8 @@ def main():
             return
         print(json.dumps(run_reference(args, ws, rank)))
         return
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if ws > 1 else None
+    if ws > 1:  # one GPU per rank, chosen before the library initialises CUDA
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
     out = run_ours(args, ws, rank, local)
     if rank == 0:
         print(json.dumps(out))
