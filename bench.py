@@ -33,6 +33,11 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# DRAM bytes (read + write) of one launch of the dominant gradient kernel,
+# from an ncu capture of `python bench.py --case grad --workload W --precision P`
+# (one launch, dram__bytes_read.sum + dram__bytes_write.sum).
+TRAFFIC = {}
+
 WORKLOADS = {
     "logistic_100k": dict(kind="logistic_100k", chains=1024, warmup=500, samples=1000),
     "logistic_1k": dict(kind="logistic", chains=4, warmup=1000, samples=1000),
@@ -46,6 +51,25 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def select_device(ws, local):
+    """One GPU per rank, chosen before the library initialises CUDA: the
+    local-th entry of an existing CUDA_VISIBLE_DEVICES list (a launcher or
+    scheduler may have set one), else GPU `local`.  Returns the device as
+    nvidia-smi names it (index or UUID), for the clock sampler."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if ws <= 1:
+        return (vis.split(",")[0].strip() if vis else "0")
+    if vis:
+        lst = [v.strip() for v in vis.split(",") if v.strip()]
+        if local >= len(lst):
+            raise RuntimeError(f"local rank {local} has no GPU in CUDA_VISIBLE_DEVICES={vis}")
+        dev = lst[local]
+    else:
+        dev = str(local)
+    os.environ["CUDA_VISIBLE_DEVICES"] = dev
+    return dev
 
 
 class ClockSampler:
@@ -159,7 +183,7 @@ def cpu_baseline(ds, wl, seconds_target=20.0, stepsize=None, inv_metric=None):
                       f"(one chain per core, FP64, {g} gradient evaluations in {dt:.1f} s)"}
 
 
-def run_ours(args, ws, rank, local):
+def run_ours(args, ws, rank, gpu):
     from stan_gb300 import Model, _lib, sampler, workloads
     wl = WORKLOADS[args.workload]
     ds = workloads.make_dataset(wl["kind"], seed=1 + rank)
@@ -176,7 +200,7 @@ def run_ours(args, ws, rank, local):
     grad_ms = []
     steps = 0
     launches = 0
-    with ClockSampler(local) as clk:
+    with ClockSampler(gpu) as clk:
         t_wall = time.time()
         for i in range(args.steps):
             flush_l2()
@@ -204,14 +228,16 @@ def run_ours(args, ws, rank, local):
     peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0))
     ach = flops / (mean_ms * 1e-3) / 1e12
     kpad = 16 * ((K + 1 + 15) // 16)
-    executed = 3 * 2 * 2.0 * N * C * kpad  # three bf16 products, two contractions, K padded
+    tensor = args.precision in ("bf16x3", "f16x3")
+    executed = 3 * 2 * 2.0 * N * C * kpad  # three 16-bit products, two contractions, K padded
+    traffic = TRAFFIC.get((args.workload, args.precision))
     roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
             "frac": ach / peak,
             # dram__bytes_read.sum + dram__bytes_write.sum of one launch
-            # (profiles/glm_tct_kernel_logistic_100k_1024chains.md)
-            "traffic": 5.70e7 if args.precision == "bf16x3" else None,
+            "traffic": traffic[0] if traffic else None,
+            "traffic_source": traffic[1] if traffic else None,
             "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)",
-            "kernel": "glm_tct_kernel" if args.precision == "bf16x3" else "loglik_partial_pool_kernel",
+            "kernel": "glm_tct_kernel" if tensor else "loglik_partial_pool_kernel",
             "executed_tflops": executed / (mean_ms * 1e-3) / 1e12,
             "executed_frac": executed / (mean_ms * 1e-3) / 1e12 / peak,
             "mean_launch_ms": mean_ms,
@@ -515,7 +541,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="logistic_100k", choices=list(WORKLOADS))
-    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "fp32", "bf16x3"])
+    ap.add_argument("--precision", default="f16x3", choices=["fp64", "fp32", "bf16x3", "f16x3"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -546,9 +572,8 @@ def main():
             return
         print(json.dumps(run_reference(args, ws, rank)))
         return
-    if ws > 1:  # one GPU per rank, chosen before the library initialises CUDA
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
-    out = run_ours(args, ws, rank, local)
+    gpu = select_device(ws, local)
+    out = run_ours(args, ws, rank, gpu)
     if rank == 0:
         print(json.dumps(out))
 

@@ -59,10 +59,20 @@ enum { GBNUTS_F64 = 0, GBNUTS_F32 = 1, GBNUTS_BF16 = 2 };
  *           cores with FP32 accumulation (three products per contraction),
  *           totals and sampler state in double precision.
  *  BF16   : the same contractions as single bf16 products (no lo parts).
+ *  F16X3  : the BF16X3 products on fp16 hi/lo parts (22 significant bits per
+ *           operand instead of 16, same tensor-core rate), with exact
+ *           power-of-two scales keeping every part inside the fp16 range;
+ *           logistic GLM with up to 127 features.
  *  The bf16 forms take the logistic and Poisson GLMs: up to 127 features on
  *  the tensor-memory kernel, wider designs as bf16 GEMMs around a link
  *  kernel. */
-enum { GBNUTS_PREC_FP64 = 0, GBNUTS_PREC_FP32 = 1, GBNUTS_PREC_BF16X3 = 2, GBNUTS_PREC_BF16 = 3 };
+enum {
+  GBNUTS_PREC_FP64 = 0,
+  GBNUTS_PREC_FP32 = 1,
+  GBNUTS_PREC_BF16X3 = 2,
+  GBNUTS_PREC_BF16 = 3,
+  GBNUTS_PREC_F16X3 = 4
+};
 
 typedef struct gbnuts_model gbnuts_model;
 
@@ -383,6 +393,15 @@ int gbnuts_summary_device(const double* d_draws, int num_chains, int max_rows, i
                           double* d_out, void* stream);
 int gbnuts_summary(const double* draws, int num_chains, int max_rows, int n_cols, int row_begin,
                    int n_rows, int col_begin, int n_quantities, double* out);
+
+/* Launch-shape overrides, for tuning (no counterpart in the reference).
+ * Process-wide; 0 restores the built-in rule.  split_rows_min: minimum rows
+ * per row split of the CUDA-core gradient (fp64 / fp32 forms); team_warps:
+ * warps per chain of the step kernel (1, 2 or 4).  A fit's splits fix the
+ * order of its gradient sums, so a setting changes draws at round-off level
+ * (runs stay deterministic for a fixed setting); change it between runs, not
+ * while one is going.  USAGE for a team_warps other than 0, 1, 2, 4. */
+int gbnuts_set_launch_shape(long long split_rows_min, int team_warps);
 
 /* Device and build information: writes a short text description. */
 int gbnuts_device_info(char* buf, int cap);

@@ -10,13 +10,6 @@
 extern "C" {
 #endif
 
-/* One tile through the tensor-core contraction layouts used by the bf16x3
- * gradient: D1 = A . B^T and D2 = A^T . R with A 128x128, B 64x128 and
- * R 128x64 bf16 matrices (row-major uint16 bit patterns), D1 and D2 128x64
- * fp32 outputs.  Returns 0 on success. */
-int gbnuts_tc_probe(const uint16_t* A, const uint16_t* B, const uint16_t* R, float* D1,
-                    float* D2);
-
 /* The chains-on-M layouts: D1 = A . X^T and D2 = R . X with A and R held in
  * tensor memory (128 lanes x 64 32-bit words each, Aw / Rw, written as given:
  * two bf16 per word) and X a 128x128 bf16 matrix (row-major uint16 bit

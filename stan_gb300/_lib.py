@@ -12,9 +12,10 @@ LIB_PATH = os.path.join(_HERE, "_build", "libgbnuts.so")
 OK, USAGE, DATAERR, NOINPUT, SOFTWARE, CONFIG = 0, 64, 65, 66, 70, 78
 LOGISTIC, POISSON, HIER_NORMAL, HIER_LOGISTIC = 1, 2, 3, 4
 F64, F32, BF16 = 0, 1, 2
-PREC_FP64, PREC_FP32, PREC_BF16X3, PREC_BF16 = 0, 1, 2, 3
+PREC_FP64, PREC_FP32, PREC_BF16X3, PREC_BF16, PREC_F16X3 = 0, 1, 2, 3, 4
 METRIC_DIAG, METRIC_DENSE = 0, 1
-PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "bf16x3": PREC_BF16X3, "bf16": PREC_BF16}
+PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "bf16x3": PREC_BF16X3, "bf16": PREC_BF16,
+              "f16x3": PREC_F16X3}
 INIT_WRITER, SAMPLE_WRITER, DIAGNOSTIC_WRITER = 0, 1, 2
 CHAIN_STATUS = {0: "ok", 1: "init_failed", 2: "stepsize_init_failed", 3: "stepsize_failed",
                 4: "metric_overflow", 5: "interrupted", 6: "bad_metric"}
@@ -143,6 +144,7 @@ SIGNATURES = {
                                        ctypes.POINTER(Callbacks),
                                        ctypes.POINTER(ctypes.c_void_p)]),
     "gbnuts_csv_close": (ctypes.c_int, [ctypes.c_void_p]),
+    "gbnuts_set_launch_shape": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int]),
     "gbnuts_device_info": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "gbnuts_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
 }

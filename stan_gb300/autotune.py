@@ -1,15 +1,16 @@
 """Offline autotuner for the launch shapes of the CUDA-core gradient and the step kernel.
 
-Two knobs decide how a fit's work is cut into launches:
+Two knobs decide how a fit's work is cut into launches, both set through
+the library's gbnuts_set_launch_shape(split_rows_min, team_warps):
 
-  GBNUTS_SPLIT_ROWS  minimum rows per split of the CUDA-core partial kernel
-                     (fp64 / fp32 forms; splits are also bounded by about two
-                     waves of CTAs over the 152 SMs and, for the hierarchical
-                     families, by the group count)
-  GBNUTS_TEAM_WARPS  warps per chain of the step kernel (1, 2 or 4; by default
-                     1 up to D = 64, 2 up to 1024, 4 above)
+  split_rows_min  minimum rows per split of the CUDA-core partial kernel
+                  (fp64 / fp32 forms; splits are also bounded by about two
+                  waves of CTAs over the device's SMs and, for the
+                  hierarchical families, by the group count)
+  team_warps      warps per chain of the step kernel (1, 2 or 4; by default
+                  1 up to D = 64, 2 up to 1024, 4 above)
 
-Both are read once per process, so each candidate runs in its own process: a
+The setting is process-wide, so each candidate runs in its own process: a
 short adaptive fit of the workload, timed with CUDA events (device ms per
 step).  The tuner prints the table and the best candidate and can write them
 as JSON.  The library's built-in rules were set from such sweeps; the knobs
@@ -35,7 +36,9 @@ TEAM_WARPS = (1, 2, 4)
 
 def _candidate(args):
     """Runs in the child process: one short fit, prints its timing as JSON."""
-    from stan_gb300 import Model, sampler, workloads
+    from stan_gb300 import Model, _lib, sampler, workloads
+    _lib.check(_lib.load().gbnuts_set_launch_shape(args.split_rows, args.team_warps),
+               "gbnuts_set_launch_shape")
     ds = workloads.make_dataset(args.workload, seed=1)
     m = Model.from_dataset(ds)
     kw = dict(num_chains=args.chains, num_warmup=args.iters, num_samples=0,
@@ -51,11 +54,10 @@ def sweep(workload, chains, precision, iters=30, split_rows=SPLIT_ROWS, team_war
     """Times every (split_rows, team_warps) candidate; returns (rows, best)."""
     rows = []
     for sr, tw in itertools.product(split_rows, team_warps):
-        env = dict(os.environ, GBNUTS_SPLIT_ROWS=str(sr), GBNUTS_TEAM_WARPS=str(tw))
         cmd = [python, "-m", "stan_gb300.autotune", "--child", "--workload", workload,
-               "--chains", str(chains), "--precision", precision, "--iters", str(iters)]
-        r = subprocess.run(cmd, env=env, cwd=_ROOT, capture_output=True, text=True,
-                           timeout=timeout)
+               "--chains", str(chains), "--precision", precision, "--iters", str(iters),
+               "--split-rows", str(sr), "--team-warps", str(tw)]
+        r = subprocess.run(cmd, cwd=_ROOT, capture_output=True, text=True, timeout=timeout)
         if r.returncode != 0:
             rows.append({"split_rows": sr, "team_warps": tw, "error": r.stderr[-300:]})
             continue
@@ -70,7 +72,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--workload", default="hier_normal")
     ap.add_argument("--chains", type=int, default=256)
-    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "bf16x3"])
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "bf16x3", "f16x3"])
     ap.add_argument("--iters", type=int, default=30)
     ap.add_argument("--split-rows", default=",".join(map(str, SPLIT_ROWS)))
     ap.add_argument("--team-warps", default=",".join(map(str, TEAM_WARPS)))
@@ -78,6 +80,8 @@ def main(argv=None):
     ap.add_argument("--child", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args(argv)
     if args.child:
+        args.split_rows = int(args.split_rows)
+        args.team_warps = int(args.team_warps)
         _candidate(args)
         return
     rows, best = sweep(args.workload, args.chains, args.precision, args.iters,

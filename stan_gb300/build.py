@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgbnuts.so")
-SOURCES = ["loglik.cu", "nuts.cu", "capi.cu", "glm_tc.cu", "noalloc.cu", "pool.cu", "glm_tct.cu",
+SOURCES = ["loglik.cu", "nuts.cu", "capi.cu", "noalloc.cu", "pool.cu", "glm_tct.cu",
            "glm_gemm.cu", "ess.cu", "csv.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

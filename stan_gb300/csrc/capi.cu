@@ -20,6 +20,8 @@
 #include <vector>
 #include <thread>
 #include <atomic>
+#include <map>
+#include <mutex>
 
 #include "../../include/gbnuts.h"
 #include "gbnuts_internal.h"
@@ -31,15 +33,60 @@ namespace gbn {
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& s) { g_last_error = s; }
 const std::string& last_error() { return g_last_error; }
+
+static std::mutex g_dev_mu;
+
+int ensure_smem_attr(const void* kernel, size_t bytes) {
+  int dev = 0;
+  GBN_CUDA_TRY(cudaGetDevice(&dev));
+  static std::map<std::pair<int, const void*>, size_t> done;
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  size_t& have = done[{dev, kernel}];
+  if (bytes > have) {
+    GBN_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)bytes));
+    have = bytes;
+  }
+  return GBNUTS_OK;
+}
+
+int device_sm_count() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  static std::map<int, int> count;
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  auto it = count.find(dev);
+  if (it != count.end()) return it->second;
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+    n = 1;
+  count[dev] = n;
+  return n;
+}
 }  // namespace gbn
 
 using namespace gbn;
 
-// Builds the tensor-core tiles of X on first use of the bf16x3 form.
+// Builds the tensor-core tiles of X on first use of a tensor-core form.
 static int ensure_precision(gbnuts_model* m, int precision) {
-  if (precision < GBNUTS_PREC_FP64 || precision > GBNUTS_PREC_BF16)
+  if (precision < GBNUTS_PREC_FP64 || precision > GBNUTS_PREC_F16X3)
     return fail(GBNUTS_USAGE, "unknown precision");
   if (!is_tensor_precision(precision)) return GBNUTS_OK;
+  if (precision == GBNUTS_PREC_F16X3) {
+    if (m->desc.link != LINK_LOGIT || !tc_supported(m->desc))
+      return fail(GBNUTS_USAGE,
+                  "the f16x3 form takes the logistic GLM with up to 127 features");
+    if (m->d_tc_xt16) return GBNUTS_OK;
+    int tiles = 0, x_exp = 0;
+    int rc = tc_prepare(m->desc, true, &m->d_tc_xt16, &m->d_tc_yt, &tiles, &x_exp, m->stream);
+    if (rc) return rc;
+    GBN_CUDA_TRY(cudaStreamSynchronize(m->stream));
+    m->desc.tc_xt16 = m->d_tc_xt16;
+    m->desc.tc_x_exp = x_exp;
+    m->desc.tc_yt = m->d_tc_yt;
+    m->desc.tc_tiles = tiles;
+    return GBNUTS_OK;
+  }
   if (!tc_supported(m->desc) && tensor_form_supported(m->desc)) {
     // wide design: bf16 copies of X for the GEMM form
     if (m->d_gx_h) return GBNUTS_OK;
@@ -54,8 +101,8 @@ static int ensure_precision(gbnuts_model* m, int precision) {
     return fail(GBNUTS_USAGE,
                 "the bf16 tensor-core forms need a logistic or Poisson GLM");
   if (m->d_tc_xt) return GBNUTS_OK;
-  int tiles = 0;
-  int rc = tc_prepare(m->desc, &m->d_tc_xt, &m->d_tc_yt, &tiles, m->stream);
+  int tiles = 0, x_exp = 0;
+  int rc = tc_prepare(m->desc, false, &m->d_tc_xt, &m->d_tc_yt, &tiles, &x_exp, m->stream);
   if (rc) return rc;
   GBN_CUDA_TRY(cudaStreamSynchronize(m->stream));
   m->desc.tc_xt = m->d_tc_xt;
@@ -116,6 +163,15 @@ int gbnuts_internal_model_view(const gbnuts_model* m, gbn::ModelDesc* desc,
 }
 
 extern "C" {
+
+int gbnuts_set_launch_shape(long long split_rows_min, int team_warps) {
+  if (split_rows_min < 0 || !(team_warps == 0 || team_warps == 1 || team_warps == 2 ||
+                              team_warps == 4))
+    return fail(GBNUTS_USAGE, "split_rows_min >= 0 and team_warps in {0, 1, 2, 4}");
+  set_split_rows_min(split_rows_min);
+  set_team_warps(team_warps);
+  return GBNUTS_OK;
+}
 
 int gbnuts_last_error(char* buf, int cap) {
   if (!buf || cap <= 0) return -1;
@@ -271,6 +327,7 @@ void gbnuts_model_destroy(gbnuts_model* m) {
   if (!m) return;
   free_workspace(m->ws);
   if (m->d_tc_xt) cudaFree(m->d_tc_xt);
+  if (m->d_tc_xt16) cudaFree(m->d_tc_xt16);
   if (m->d_tc_yt) cudaFree(m->d_tc_yt);
   if (m->d_gx_h) cudaFree(m->d_gx_h);
   if (m->d_gx_l) cudaFree(m->d_gx_l);
@@ -665,10 +722,11 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
       if (ws) ws->tc_words = nullptr;
     }
   } words_guard;
-  if (is_tensor_precision(rc->precision) && m->desc.tc_xt &&
-      (tc_chains_on_m() || rc->precision == GBNUTS_PREC_BF16)) {
+  if (is_tensor_precision(rc->precision) &&
+      (rc->precision == GBNUTS_PREC_F16X3 ? m->desc.tc_xt16 : m->desc.tc_xt)) {
     GBN_CUDA_TRY(dr.alloc(&d_reqw, (size_t)C * tc::kThetaWords));
     h_fit.f.req_tc = d_reqw;
+    h_fit.f.req_tc_f16 = rc->precision == GBNUTS_PREC_F16X3 ? 1 : 0;
     m->ws.tc_words = d_reqw;
     words_guard.ws = &m->ws;
   }

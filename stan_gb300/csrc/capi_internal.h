@@ -29,6 +29,7 @@ struct gbnuts_model {
   int scratch_C = 0;
   cudaStream_t stream = nullptr;
   void* d_tc_xt = nullptr;
+  void* d_tc_xt16 = nullptr;
   float* d_tc_yt = nullptr;
   void* d_gx_h = nullptr;
   void* d_gx_l = nullptr;

@@ -401,12 +401,8 @@ int launch_summary(const char* who, const double* d_draws, int num_chains, int m
     return GBNUTS_USAGE;
   }
   const size_t smem = (size_t)kMaxValues * (8 + 8 + 4);
-  static bool attr = false;
-  if (!attr) {
-    GBN_CUDA_TRY(cudaFuncSetAttribute(summary_kernel<FULL>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  int rc = ensure_smem(summary_kernel<FULL>, smem);
+  if (rc) return rc;
   summary_kernel<FULL><<<n_quantities, kThreads, smem, st>>>(
       d_draws, num_chains, max_rows, n_cols, row_begin, n_rows, col_begin, d_out);
   GBN_CUDA_TRY(cudaGetLastError());

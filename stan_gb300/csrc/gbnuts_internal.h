@@ -21,6 +21,17 @@ namespace gbn {
 void set_last_error(const std::string& s);
 const std::string& last_error();
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device.  Kept per (device, kernel) and guarded by a mutex, so every
+// device a process uses gets the opt-in and host threads may launch at once.
+int ensure_smem_attr(const void* kernel, size_t bytes);
+template <typename F>
+inline int ensure_smem(F* kernel, size_t bytes) {
+  return ensure_smem_attr(reinterpret_cast<const void*>(kernel), bytes);
+}
+// Multiprocessor count of the current device (queried once per device).
+int device_sm_count();
+
 enum Link { LINK_LOGIT = 0, LINK_POISSON_LOG = 1, LINK_NORMAL = 2 };
 
 // A log density on the device.  theta layout per family:
@@ -45,8 +56,11 @@ struct ModelDesc {
   double s_base, s_tau, s_sigma, s_beta;  // prior scales
   double r_base2, r_tau2, r_sigma2, r_beta2;  // 1 / scale^2 (set with the scales)
   double sum_lgamma_y;                    // Poisson constant, for propto = false
-  // tensor-core form: X pre-tiled as bf16 hi/lo (128-row tiles), y per tile row
+  // tensor-core forms: X pre-tiled as bf16 hi/lo (128-row tiles), as fp16
+  // hi/lo of x 2^tc_x_exp for the f16x3 form, y per tile row
   const void* tc_xt;
+  const void* tc_xt16;
+  int tc_x_exp;
   const float* tc_yt;
   int tc_tiles;
   // wide-design tensor-core form: X as row-major bf16 hi (and lo) copies
@@ -134,19 +148,18 @@ int fit_ess(const double* d_draws, int C, int max_rows, int n_cols, int row_begi
 // and C rounded up to 4, 8 or 16): fewer idle threads for small fits.
 int block_chains(int K, int C);
 
-// Tensor-core (bf16 hi/lo) GLM path.
-int tc_max_features();
-int tc_splits(const ModelDesc& m, int C);
-int tc_prepare(const ModelDesc& m, void** xt, float** yt, int* n_tiles, cudaStream_t st);
-int launch_tc(const ModelDesc& m, const double* Q, int ldq, int C, const int* active,
-              GradWorkspace& ws, cudaStream_t st);
-// Chains-on-M form (Theta and R as tensor-memory operands, 128 chains per CTA).
+// Tensor-core GLM path, chains on M (Theta and R as tensor-memory operands,
+// 128 chains per CTA).  tc_prepare builds the X tiles (f16: the fp16 tiles
+// and their scale exponent x_exp) and, when *yt is null, y per tile row.
+int tc_prepare(const ModelDesc& m, bool f16, void** xt, float** yt, int* n_tiles, int* x_exp,
+               cudaStream_t st);
 int tct_splits(const ModelDesc& m, int C);
 int launch_tct(const ModelDesc& m, int precision, const double* Q, int ldq, int C,
                const int* active, GradWorkspace& ws, cudaStream_t st);
-// Which tensor-core kernel the bf16x3 form uses (GBNUTS_TC_KERNEL=m64 selects
-// the chains-on-N kernel, for comparisons).
-bool tc_chains_on_m();
+// Minimum rows per split of the CUDA-core gradient (0: the built-in rule).
+void set_split_rows_min(long long rows);
+// Warps per chain of the step kernel (0: the built-in rule).
+void set_team_warps(int w);
 // Whether the model can use the tensor-memory kernel (K + intercept <= 128).
 inline bool tc_supported(const ModelDesc& m) {
   return (m.link == LINK_LOGIT || m.link == LINK_POISSON_LOG) && m.off_z < 0 &&
@@ -156,7 +169,7 @@ inline bool tc_supported(const ModelDesc& m) {
 inline bool tensor_form_supported(const ModelDesc& m) {
   return (m.link == LINK_LOGIT || m.link == LINK_POISSON_LOG) && m.off_z < 0;
 }
-inline bool is_tensor_precision(int p) { return p == 2 || p == 3; }
+inline bool is_tensor_precision(int p) { return p == 2 || p == 3 || p == 4; }
 // Wide-design form (glm_gemm.cu): bf16 GEMMs around a link kernel.
 int gemm_kpad(const ModelDesc& m);
 int gemm_prepare(const ModelDesc& m, void** xh, void** xl, cudaStream_t st);

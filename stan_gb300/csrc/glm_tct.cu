@@ -1,5 +1,6 @@
 // Batched GLM log density and gradient on the tcgen05 tensor cores, chains on
-// the M dimension (precision GBNUTS_PREC_BF16X3, logistic and Poisson).
+// the M dimension (precisions GBNUTS_PREC_BF16X3 and GBNUTS_PREC_BF16 for the
+// logistic and Poisson GLMs, GBNUTS_PREC_F16X3 for the logistic GLM).
 //
 // A CTA owns 128 chains (one per TMEM lane) and a range of 128-row tiles of X,
 // one tile per pass:
@@ -18,13 +19,27 @@
 // Each epilogue thread owns one chain, so the lp sum over rows stays in the
 // thread (a compensated fp32 sum).
 //
+// The fp16 form (F16X3) runs the same products on fp16 hi/lo parts: 11 + 11
+// significant bits per operand instead of 8 + 8, so the split represents each
+// operand to about 2^-22 instead of 2^-17, at the same tensor-core rate.  The
+// narrower fp16 exponent range is handled with exact power-of-two scales:
+// X is stored times 2^sx (largest |x| in [2^13, 2^14), one sx per model),
+// each chain's theta times 2^-e_c (largest |theta_k log2 e| in [2^13, 2^14),
+// e_c computed with theta), the residual (|r| <= 1 for the logistic link)
+// times 2^14; the epilogue multiplies eta by 2^(e_c - sx) and the gradient by
+// 2^-(sx + 14).
+//
 // TMEM columns (512): eta^T [0, 128), G^T [128, 256), Theta hi [256, 320) and
 // lo [320, 384), R hi [384, 448) and lo [448, 512).  Shared memory: a 3-stage
 // ring of 128-row X tiles (hi + lo + y, 65 KiB each).
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <math.h>
 
+#include <string.h>
+
 #include <algorithm>
+#include <string>
 
 #include "../../include/gbnuts.h"
 #include "gbnuts_internal.h"
@@ -71,10 +86,11 @@ __device__ __forceinline__ uint64_t desc_feats(uint32_t part, int ks) {
 }  // namespace tct
 
 struct TctArgs {
-  const __nv_bfloat16* xt;  // pre-tiled X (hi/lo per 128-row tile)
-  const float* yt;          // y per tile row
+  const uint16_t* xt;  // pre-tiled X (16-bit hi/lo parts per 128-row tile)
+  const float* yt;     // y per tile row
   long long N;
   int K, has_base, n_tiles;
+  int x_exp;           // fp16 form: X is stored times 2^x_exp
   const double* Q;
   const uint32_t* QW;  // theta as packed words (kThetaWords per chain), or null
   int ldq, C;
@@ -94,8 +110,9 @@ enum { B_XFULL = 0, B_XEMPTY = 3, B_D1FULL = 6, B_D1EMPTY = 7, B_RFULL = 8, B_RE
 // rr0 + j, y[j] their outcomes.  Accumulates pa, pb with lp = ln2 pa - pb
 // (logistic: pa = sum y e2 - max(e2, 0) - log2(1 + 2^-|e2|), pb = 0;
 // Poisson: pa = sum y e2, pb = sum mu) and packs r = y - mean as bf16 hi / lo
-// pairs.  MASK: rows j >= nvalid (past N) contribute nothing.
-template <int LINK, bool MASK, int RWN>
+// pairs (F16: 2^14 r as fp16 hi / lo pairs).  MASK: rows j >= nvalid (past N)
+// contribute nothing.
+template <int LINK, bool MASK, int RWN, bool F16>
 __device__ __forceinline__ void epilogue_values(const float* e2, const float* y, int nvalid,
                                                 float& pa, float& pb, uint32_t* wh,
                                                 uint32_t* wl) {
@@ -132,11 +149,20 @@ __device__ __forceinline__ void epilogue_values(const float* e2, const float* y,
     }
 #pragma unroll
     for (int e = 0; e < 4; e += 2) {
-      const __nv_bfloat162 hp = __floats2bfloat162_rn(res[e], res[e + 1]);
-      const float2 hf = __bfloat1622float2(hp);
-      const __nv_bfloat162 lo = __floats2bfloat162_rn(res[e] - hf.x, res[e + 1] - hf.y);
-      wh[(j + e) >> 1] = *reinterpret_cast<const uint32_t*>(&hp);
-      wl[(j + e) >> 1] = *reinterpret_cast<const uint32_t*>(&lo);
+      if (F16) {
+        const float r0 = res[e] * 16384.f, r1 = res[e + 1] * 16384.f;
+        const __half2 hp = __floats2half2_rn(r0, r1);
+        const float2 hf = __half22float2(hp);
+        const __half2 lo = __floats2half2_rn(r0 - hf.x, r1 - hf.y);
+        wh[(j + e) >> 1] = *reinterpret_cast<const uint32_t*>(&hp);
+        wl[(j + e) >> 1] = *reinterpret_cast<const uint32_t*>(&lo);
+      } else {
+        const __nv_bfloat162 hp = __floats2bfloat162_rn(res[e], res[e + 1]);
+        const float2 hf = __bfloat1622float2(hp);
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(res[e] - hf.x, res[e + 1] - hf.y);
+        wh[(j + e) >> 1] = *reinterpret_cast<const uint32_t*>(&hp);
+        wl[(j + e) >> 1] = *reinterpret_cast<const uint32_t*>(&lo);
+      }
     }
   }
 }
@@ -151,8 +177,9 @@ __device__ __forceinline__ void two_sum_add(float2& s, float v) {
 }
 
 // SPLIT: the hi/lo split products (bf16x3); otherwise one bf16 product per
-// contraction (the plain bf16 form; X's lo part unused).
-template <int LINK, bool XLO, bool SPLIT>
+// contraction (the plain bf16 form; X's lo part unused).  F16: fp16 operands
+// with the scales described above (used with XLO and SPLIT).
+template <int LINK, bool XLO, bool SPLIT, bool F16>
 __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
   using namespace tct;
   extern __shared__ unsigned char smem_raw[];
@@ -213,7 +240,7 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
           const int st = i % STAGES, u = i / STAGES;
           if (!mbar_wait_abortable(&bars[B_XEMPTY + st], (u & 1) ^ 1, abort_s, a.err, 21)) break;
           unsigned char* dst = sm + SMEM_X + st * STAGE_BYTES;
-          const __nv_bfloat16* src = a.xt + (size_t)(2 * (t_begin + i)) * (TM * TK);
+          const uint16_t* src = a.xt + (size_t)(2 * (t_begin + i)) * (TM * TK);
           mbar_arrive_expect_tx(&bars[B_XFULL + st], x_bytes + Y_BYTES);
           bulk_copy_g2s(dst, src, PART_BYTES, &bars[B_XFULL + st]);
           if (kXlo)
@@ -226,8 +253,8 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
     } else if (warp == 1) {
       // ---- MMA issuer: GEMM1 of tile i, then GEMM2 of tile i - 1
       if (lane == 0) {
-        const uint32_t id1 = make_idesc_bf16(NCH, TM, 0, 0);
-        const uint32_t id2 = make_idesc_bf16(NCH, nf, 0, 1);
+        const uint32_t id1 = make_idesc_bf16(NCH, TM, 0, 0, F16);
+        const uint32_t id2 = make_idesc_bf16(NCH, nf, 0, 1, F16);
         bool ok = mbar_wait_abortable(&bars[B_THETA], 0, abort_s, a.err, 22);
         fence_after_sync();
         auto gemm2 = [&](int i) -> bool {
@@ -279,11 +306,26 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
       const int sub = (warp - 2) >> 2;
       const int c = 32 * q + lane;
       const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
-      // log2(e) Theta of this chain -> TMEM as bf16 hi / lo pairs (fp32 split)
+      // log2(e) Theta of this chain -> TMEM as bf16 hi / lo pairs (fp32 split),
+      // or for F16 as fp16 hi / lo pairs at the chain's scale 2^-e_c
+      float eta_scale = 1.f;
       {
         const bool act = act_s[c] != 0;
         const double* th = a.Q + (size_t)(act ? c0 + c : 0) * a.ldq;
         const uint32_t* tw = a.QW ? a.QW + (size_t)(act ? c0 + c : 0) * kThetaWords : nullptr;
+        int e_c = 0;
+        if (F16 && act) {
+          if (tw) {
+            e_c = (int)tw[kThetaExpWord];
+          } else {
+            float fmax = 0.f;
+            for (int k = 0; k < Kx; ++k) fmax = fmaxf(fmax, fabsf(theta_f32(th[k])));
+            e_c = theta_exp_f16(fmax);
+          }
+          const int es = max(-126, min(126, e_c - a.x_exp));
+          eta_scale = exp2_int(es);
+        }
+        const float th_scale = exp2_int(-e_c);
 #pragma unroll
         for (int part = 0; part < FW / 32; ++part) {
           uint32_t wh[16], wl[16];
@@ -301,8 +343,12 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
               const int k = FW * sub + 32 * part + 2 * j;
-              theta_words((act && k < Kx) ? th[k] : 0.0, (act && k + 1 < Kx) ? th[k + 1] : 0.0,
-                          wh[j], wl[j]);
+              const double d0 = (act && k < Kx) ? th[k] : 0.0;
+              const double d1 = (act && k + 1 < Kx) ? th[k + 1] : 0.0;
+              if (F16)
+                theta_words_f16(theta_f32(d0), theta_f32(d1), th_scale, wh[j], wl[j]);
+              else
+                theta_words(d0, d1, wh[j], wl[j]);
             }
           }
           tmem_st16(lane_addr + COL_TH + FW / 2 * sub + 16 * part, wh);
@@ -325,6 +371,10 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
         float v[RW];
         tmem_ld32(lane_addr + COL_D1 + RW * sub, v);
         tmem_ld_wait();
+        if (F16) {
+#pragma unroll
+          for (int j = 0; j < RW; ++j) v[j] *= eta_scale;
+        }
         fence_before_sync();
         __syncwarp();
         if (lane == 0) mbar_arrive(&bars[B_D1EMPTY]);
@@ -336,9 +386,9 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
         float pa = 0.f, pb = 0.f;
         uint32_t wh[RW / 2], wl[RW / 2];
         if (nvalid == RW)
-          epilogue_values<LINK, false, RW>(v, ys, RW, pa, pb, wh, wl);
+          epilogue_values<LINK, false, RW, F16>(v, ys, RW, pa, pb, wh, wl);
         else
-          epilogue_values<LINK, true, RW>(v, ys, nvalid, pa, pb, wh, wl);
+          epilogue_values<LINK, true, RW, F16>(v, ys, nvalid, pa, pb, wh, wl);
         two_sum_add(sa, pa);
         if (LINK != LINK_LOGIT) two_sum_add(sb, pb);
         if (!warp_wait(&bars[B_REMPTY], (i & 1) ^ 1, abort_s, a.err, 27)) {
@@ -362,6 +412,11 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
 #pragma unroll
         for (int j = 0; j < FW; j += 32) tmem_ld32(lane_addr + COL_D2 + FW * sub + j, g + j);
         tmem_ld_wait();
+        if (F16) {
+          const float gs = exp2_int(max(-126, min(126, -a.x_exp - 14)));
+#pragma unroll
+          for (int j = 0; j < FW; ++j) g[j] *= gs;
+        }
         if (act_s[c]) {
           double* dst = a.P + ((size_t)s * a.C + c0 + c) * a.NP;
 #pragma unroll
@@ -398,21 +453,153 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
 
 int tct_splits(const ModelDesc& m, int C) {
   const int groups = (C + tct::NCH - 1) / tct::NCH;
-  int S = std::max(1, 148 / groups);
+  int S = std::max(1, device_sm_count() / groups);
   S = std::min<long long>(S, std::max(1, m.tc_tiles));
   return S;
 }
 
-template <int LINK, bool XLO, bool SPLIT>
+// ------------------------------------------------------------------ tiles
+// X as 128-row tiles, each a hi part then a lo part of 128 x 128 16-bit
+// values in the canonical K-major core-matrix layout (feature 0 is the
+// intercept's constant 1 when the model has one), and y per tile row.
+// F16: the parts are fp16 of x 2^x_exp; otherwise bf16 of x.
+template <bool F16>
+__global__ void tct_tiles_kernel(const void* X, int x_dtype, long long N, int K, int has_base,
+                                 int n_tiles, uint16_t* xt, float scale) {
+  using namespace tct;
+  const long long total = (long long)n_tiles * TM * TK;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long t = i / (TM * TK);
+    const int e = (int)(i - t * (TM * TK));
+    const int r = e / TK, k = e - r * TK;
+    const long long row = t * TM + r;
+    float v = 0.f;
+    if (row < N) {
+      if (k < has_base) {
+        v = 1.f;
+      } else if (k - has_base < K) {
+        const long long idx = row * K + (k - has_base);
+        if (x_dtype == GBNUTS_F64)
+          v = (float)static_cast<const double*>(X)[idx];
+        else if (x_dtype == GBNUTS_F32)
+          v = static_cast<const float*>(X)[idx];
+        else
+          v = __uint_as_float(((unsigned)static_cast<const uint16_t*>(X)[idx]) << 16);
+      }
+    }
+    uint16_t hb, lb;
+    if (F16) {
+      __half hi, lo;
+      split_f16(v * scale, hi, lo);
+      hb = __half_as_ushort(hi);
+      lb = __half_as_ushort(lo);
+    } else {
+      __nv_bfloat16 hi, lo;
+      split_bf16(v, hi, lo);
+      hb = __bfloat16_as_ushort(hi);
+      lb = __bfloat16_as_ushort(lo);
+    }
+    const uint32_t off = kmajor_off(r, k, TK) / 2;
+    xt[(2 * t) * (TM * TK) + off] = hb;
+    xt[(2 * t + 1) * (TM * TK) + off] = lb;
+  }
+}
+
+__global__ void tct_y_kernel(long long N, int n_tiles, const double* y, float* yt) {
+  const long long total = (long long)n_tiles * tct::TM;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x)
+    yt[i] = i < N ? (float)y[i] : 0.f;
+}
+
+// Largest |x| of the design (as fp32 bits; non-negative floats order like
+// their bit patterns).
+__global__ void tct_maxabs_kernel(const void* X, int x_dtype, long long n, unsigned* out) {
+  float mx = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float v;
+    if (x_dtype == GBNUTS_F64)
+      v = (float)static_cast<const double*>(X)[i];
+    else if (x_dtype == GBNUTS_F32)
+      v = static_cast<const float*>(X)[i];
+    else
+      v = __uint_as_float(((unsigned)static_cast<const uint16_t*>(X)[i]) << 16);
+    mx = fmaxf(mx, fabsf(v));
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(mx));
+}
+
+int tc_prepare(const ModelDesc& m, bool f16, void** xt, float** yt, int* n_tiles, int* x_exp,
+               cudaStream_t st) {
+  using namespace tct;
+  const int tiles = (int)((m.N + TM - 1) / TM);
+  const size_t xbytes = (size_t)tiles * 2 * PART_BYTES;
+  const int threads = 256;
+  const int grid_cap = device_sm_count() * 16;
+  float scale = 1.f;
+  *x_exp = 0;
+  if (f16) {
+    // x_exp: the largest |x| (and the intercept's 1) times 2^x_exp in [2^13, 2^14)
+    unsigned* d_mx = nullptr;
+    GBN_CUDA_TRY(cudaMalloc(&d_mx, sizeof(unsigned)));
+    GBN_CUDA_TRY(cudaMemsetAsync(d_mx, 0, sizeof(unsigned), st));
+    const long long n = m.N * (long long)m.K;
+    if (n > 0)
+      tct_maxabs_kernel<<<(int)std::min<long long>((n + threads - 1) / threads, grid_cap), threads,
+                          0, st>>>(m.X, m.x_dtype, n, d_mx);
+    unsigned bits = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, d_mx, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_mx);
+    if (e != cudaSuccess) {
+      set_last_error(std::string("design range: ") + cudaGetErrorString(e));
+      return GBNUTS_SOFTWARE;
+    }
+    float mx = 0.f;
+    memcpy(&mx, &bits, sizeof(float));
+    if (m.has_base) mx = std::max(mx, 1.f);
+    if (!(mx < 3.0e38f)) {
+      set_last_error("the fp16 form needs a finite design matrix");
+      return GBNUTS_DATAERR;
+    }
+    if (mx > 0.f) {
+      int e2 = 0;
+      frexpf(mx, &e2);
+      *x_exp = std::max(-100, std::min(100, 13 - (e2 - 1)));
+    }
+    scale = ldexpf(1.f, *x_exp);
+  }
+  GBN_CUDA_TRY(cudaMalloc(xt, xbytes));
+  const long long total = (long long)tiles * TM * TK;
+  const int blocks = (int)std::min<long long>((total + threads - 1) / threads, grid_cap);
+  if (f16)
+    tct_tiles_kernel<true><<<blocks, threads, 0, st>>>(m.X, m.x_dtype, m.N, m.K, m.has_base,
+                                                       tiles, static_cast<uint16_t*>(*xt), scale);
+  else
+    tct_tiles_kernel<false><<<blocks, threads, 0, st>>>(m.X, m.x_dtype, m.N, m.K, m.has_base,
+                                                        tiles, static_cast<uint16_t*>(*xt), scale);
+  GBN_CUDA_TRY(cudaGetLastError());
+  if (*yt == nullptr) {
+    GBN_CUDA_TRY(cudaMalloc(yt, (size_t)tiles * TM * sizeof(float)));
+    tct_y_kernel<<<std::max(1, std::min(grid_cap, (tiles * TM + threads - 1) / threads)), threads,
+                   0, st>>>(m.N, tiles, m.y, *yt);
+    GBN_CUDA_TRY(cudaGetLastError());
+  }
+  *n_tiles = tiles;
+  return GBNUTS_OK;
+}
+
+template <int LINK, bool XLO, bool SPLIT, bool F16>
 static int launch_tct_t(const TctArgs& a, dim3 grid, cudaStream_t st) {
   using namespace tct;
-  static bool attr = false;
-  if (!attr) {
-    GBN_CUDA_TRY(cudaFuncSetAttribute(glm_tct_kernel<LINK, XLO, SPLIT>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_ALLOC));
-    attr = true;
-  }
-  glm_tct_kernel<LINK, XLO, SPLIT><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
+  int rc = ensure_smem(glm_tct_kernel<LINK, XLO, SPLIT, F16>, SMEM_ALLOC);
+  if (rc) return rc;
+  glm_tct_kernel<LINK, XLO, SPLIT, F16><<<grid, THREADS, SMEM_ALLOC, st>>>(a);
   GBN_CUDA_TRY(cudaGetLastError());
   return GBNUTS_OK;
 }
@@ -420,13 +607,15 @@ static int launch_tct_t(const TctArgs& a, dim3 grid, cudaStream_t st) {
 int launch_tct(const ModelDesc& m, int precision, const double* Q, int ldq, int C,
                const int* active, GradWorkspace& ws, cudaStream_t st) {
   using namespace tct;
+  const bool f16 = precision == GBNUTS_PREC_F16X3;
   TctArgs a;
-  a.xt = static_cast<const __nv_bfloat16*>(m.tc_xt);
+  a.xt = static_cast<const uint16_t*>(f16 ? m.tc_xt16 : m.tc_xt);
   a.yt = m.tc_yt;
   a.N = m.N;
   a.K = m.K;
   a.has_base = m.has_base;
   a.n_tiles = m.tc_tiles;
+  a.x_exp = m.tc_x_exp;
   a.Q = Q;
   a.QW = ws.tc_words;
   a.ldq = ldq;
@@ -436,17 +625,28 @@ int launch_tct(const ModelDesc& m, int precision, const double* Q, int ldq, int 
   a.NP = ws.NP;
   a.S = ws.S;
   a.err = ws.err;
+  if (a.xt == nullptr || a.yt == nullptr) {
+    set_last_error("tensor-core tiles of X are not prepared for this precision");
+    return GBNUTS_SOFTWARE;
+  }
   const bool xlo = m.x_dtype != GBNUTS_BF16;
   const bool split = precision == GBNUTS_PREC_BF16X3;
   dim3 grid(ws.S, (C + NCH - 1) / NCH);
-  if (m.link == LINK_LOGIT) {
-    if (!split) return launch_tct_t<LINK_LOGIT, false, false>(a, grid, st);
-    return xlo ? launch_tct_t<LINK_LOGIT, true, true>(a, grid, st)
-               : launch_tct_t<LINK_LOGIT, false, true>(a, grid, st);
+  if (f16) {
+    if (m.link != LINK_LOGIT) {
+      set_last_error("the f16x3 form takes the logistic GLM");
+      return GBNUTS_USAGE;
+    }
+    return launch_tct_t<LINK_LOGIT, true, true, true>(a, grid, st);
   }
-  if (!split) return launch_tct_t<LINK_POISSON_LOG, false, false>(a, grid, st);
-  return xlo ? launch_tct_t<LINK_POISSON_LOG, true, true>(a, grid, st)
-             : launch_tct_t<LINK_POISSON_LOG, false, true>(a, grid, st);
+  if (m.link == LINK_LOGIT) {
+    if (!split) return launch_tct_t<LINK_LOGIT, false, false, false>(a, grid, st);
+    return xlo ? launch_tct_t<LINK_LOGIT, true, true, false>(a, grid, st)
+               : launch_tct_t<LINK_LOGIT, false, true, false>(a, grid, st);
+  }
+  if (!split) return launch_tct_t<LINK_POISSON_LOG, false, false, false>(a, grid, st);
+  return xlo ? launch_tct_t<LINK_POISSON_LOG, true, true, false>(a, grid, st)
+             : launch_tct_t<LINK_POISSON_LOG, false, true, false>(a, grid, st);
 }
 
 // ------------------------------------------------------------------ probe

@@ -21,6 +21,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <stdlib.h>
 #include <string.h>
@@ -329,17 +330,9 @@ __global__ void __launch_bounds__(128)
 }
 
 // ------------------------------------------------------------------ host side
-static std::mutex g_attr_mu;
-
 template <typename XT, typename CT, int CB>
-static void set_smem_attr(size_t bytes) {
-  static size_t done = 0;
-  std::lock_guard<std::mutex> lk(g_attr_mu);
-  if (bytes > done) {
-    cudaFuncSetAttribute(loglik_partial_kernel<XT, CT, CB>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    done = bytes;
-  }
+static int set_smem_attr(size_t bytes) {
+  return ensure_smem(loglik_partial_kernel<XT, CT, CB>, bytes);
 }
 
 static constexpr size_t kSmemBudget = 150 * 1024;
@@ -356,7 +349,7 @@ static void launch_partial(const ModelDesc& m, const double* Q, int ldq, int C,
                            const int* active, GradWorkspace& ws, cudaStream_t st) {
   const int RB = choose_rb<CT>(CB, m.K);
   const size_t smem = partial_smem_bytes<CT>(CB, m.K, RB);
-  set_smem_attr<XT, CT, CB>(smem);
+  if (set_smem_attr<XT, CT, CB>(smem)) return;  // reported by the caller's launch check
   dim3 grid(ws.S, (C + CB - 1) / CB);
   loglik_partial_kernel<XT, CT, CB><<<grid, kThreads, smem, st>>>(
       m, Q, ldq, C, active, ws.split_rows, RB, ws.partial, ws.NP, ws.gz);
@@ -397,15 +390,8 @@ size_t partial_smem(int K, int C, int rb, int precision) {
 template <typename XT, typename CT, int CB>
 static int launch_pool_t(const PoolGradFit* d_fits, const PoolWorkItem* d_items, int n_items,
                          size_t smem, cudaStream_t st) {
-  static size_t done = 0;
-  {
-    std::lock_guard<std::mutex> lk(g_attr_mu);
-    if (smem > done) {
-      GBN_CUDA_TRY(cudaFuncSetAttribute(loglik_partial_pool_kernel<XT, CT, CB>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      done = smem;
-    }
-  }
+  int rc = ensure_smem(loglik_partial_pool_kernel<XT, CT, CB>, smem);
+  if (rc) return rc;
   loglik_partial_pool_kernel<XT, CT, CB><<<n_items, kThreads, smem, st>>>(d_fits, d_items);
   GBN_CUDA_TRY(cudaGetLastError());
   return GBNUTS_OK;
@@ -433,34 +419,26 @@ int launch_partials_pool(const PoolGradFit* d_fits, const PoolWorkItem* d_items,
              : launch_pool_cb<uint16_t, float>(d_fits, d_items, n_items, cb, smem, st);
 }
 
-bool tc_chains_on_m() {
-  static const bool v = [] {
-    const char* e = getenv("GBNUTS_TC_KERNEL");
-    return !(e && strcmp(e, "m64") == 0);
-  }();
-  return v;
-}
-
-// Minimum rows of a split (GBNUTS_SPLIT_ROWS overrides it, for tuning).
+// Minimum rows of a split: the built-in 256, or the value set through
+// gbnuts_set_launch_shape (for tuning).
+static std::atomic<long long> g_split_rows_min{0};
+void set_split_rows_min(long long rows) { g_split_rows_min.store(rows > 0 ? rows : 0); }
 static long long split_rows_min() {
-  static const long long v = [] {
-    const char* e = getenv("GBNUTS_SPLIT_ROWS");
-    const long long r = e ? atoll(e) : 0;
-    return r > 0 ? r : 256LL;
-  }();
-  return v;
+  const long long r = g_split_rows_min.load();
+  return r > 0 ? r : 256LL;
 }
 
 int choose_splits(const ModelDesc& m, int C, int precision) {
   if (is_tensor_precision(precision)) {
     if (!tc_supported(m)) return 1;  // wide-design GEMM form: one partial row per chain
-    return tc_chains_on_m() ? tct_splits(m, C) : tc_splits(m, C);
+    return tct_splits(m, C);
   }
   const int CB = block_chains(m.K, C);
   const int chain_blocks = (C + CB - 1) / CB;
-  // Splits: enough CTAs for ~2 waves over 152 SMs, a minimum of rows each.
+  // Splits: enough CTAs for ~2 waves over the SMs, a minimum of rows each.
+  const int sms = device_sm_count();
   long long max_s = std::max(1LL, m.N / split_rows_min());
-  int S = (int)std::min<long long>(max_s, std::max(1, (2 * 152 + chain_blocks - 1) / chain_blocks));
+  int S = (int)std::min<long long>(max_s, std::max(1, (2 * sms + chain_blocks - 1) / chain_blocks));
   if (m.off_z >= 0) S = std::min(S, m.J);
   return std::max(S, 1);
 }
@@ -532,9 +510,7 @@ int launch_partials(const ModelDesc& m, int precision, const double* Q, int ldq,
   } else if (precision == GBNUTS_PREC_FP32) {
     dispatch_x<float>(m, Q, ldq, C, active, ws, stream);
   } else if (is_tensor_precision(precision) && m.tc_xt != nullptr) {
-    int rc = (tc_chains_on_m() || precision == GBNUTS_PREC_BF16)
-                 ? launch_tct(m, precision, Q, ldq, C, active, ws, stream)
-                 : launch_tc(m, Q, ldq, C, active, ws, stream);
+    int rc = launch_tct(m, precision, Q, ldq, C, active, ws, stream);
     if (rc) return rc;
   } else if (is_tensor_precision(precision) && m.gx_h != nullptr) {
     int rc = launch_gemm(m, precision, Q, ldq, C, active, ws, stream);

@@ -19,7 +19,13 @@
 //
 // The device address of the array is obtained once per device, with that
 // device current, on the first call made on that device; that first call
-// should therefore be made before any stream capture begins.
+// should therefore be made before any stream capture begins.  The address is
+// kept for the life of the process: a device reset (which discards the
+// module and its array) is not supported while the library is loaded.
+//
+// Per call, a one-thread-block kernel writes the split boundaries and clears
+// the error flag inside the array (nothing is copied from host memory), then
+// the gradient kernels of the regular entry point run on the same stream.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -70,6 +76,33 @@ int scratch_address(void** out) {
 
 size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
 }  // namespace
+
+// Split boundaries for S splits of N rows (rows[s] = N s / S), or for a
+// hierarchical model the first row of group J s / S (rows sorted by group,
+// so that is the count of rows whose group is below it), and a cleared
+// error flag.
+__global__ void noalloc_setup_kernel(long long N, int S, int J, const int* __restrict__ group,
+                                     long long* __restrict__ rows, int* __restrict__ err) {
+  for (int s = threadIdx.x; s <= S; s += blockDim.x) {
+    long long r;
+    if (group == nullptr) {
+      r = N * s / S;
+    } else {
+      const long long j = (long long)J * s / S;
+      long long lo = 0, hi = N;
+      while (lo < hi) {
+        const long long mid = lo + (hi - lo) / 2;
+        if (group[mid] < j)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      r = lo;
+    }
+    rows[s] = r;
+  }
+  if (threadIdx.x == 0) *err = 0;
+}
 
 }  // namespace gbn
 
@@ -128,17 +161,12 @@ extern "C" int gbnuts_log_prob_grad_batch_device_noalloc(gbnuts_model* m, int C,
   ws.gz = desc.off_z >= 0 ? reinterpret_cast<double*>(b + partial_bytes) : nullptr;
   ws.split_rows = reinterpret_cast<long long*>(b + partial_bytes + gz_bytes);
   ws.err = reinterpret_cast<int*>(b + partial_bytes + gz_bytes + split_bytes);
-  long long rows[kMaxSplits + 1];
-  for (int s = 0; s <= S; ++s) {
-    if (desc.off_z >= 0)
-      rows[s] = group_off[(long long)desc.J * s / S];
-    else
-      rows[s] = desc.N * s / S;
-  }
+  (void)group_off;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemcpyAsync(ws.split_rows, rows, (S + 1) * sizeof(long long),
-                                  cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ws.err, 0, sizeof(int), st);
+  noalloc_setup_kernel<<<1, 256, 0, st>>>(desc.N, S, desc.J,
+                                          desc.off_z >= 0 ? desc.group : nullptr,
+                                          ws.split_rows, ws.err);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_last_error(std::string("scratch set-up: ") + cudaGetErrorString(e));
     return GBNUTS_SOFTWARE;

@@ -30,6 +30,8 @@
 #include <math.h>
 #include <stdlib.h>
 
+#include <atomic>
+
 #include "../../include/gbnuts.h"
 #include "../../include/gbnuts_draw_stream.h"
 #include "gbnuts_internal.h"
@@ -210,15 +212,36 @@ static __device__ void drift_and_request(const Ctx& x, double* __restrict__ q,
 }
 
 // The request as tensor-core coefficient words (features 0..127, zeros past
-// D), for the chains-on-M gradient kernel.  Reads back the warp's own writes.
-static __device__ void pack_request_words(const Ctx& x, const double* rq, uint32_t* w) {
+// D), for the chains-on-M gradient kernel.  Reads back the team's own writes.
+// f16: fp16 hi / lo words at the chain's scale 2^-e (largest |theta log2 e|
+// in [2^13, 2^14)), e in the exponent word.
+static __device__ void pack_request_words(const Ctx& x, const double* rq, uint32_t* w,
+                                          int f16) {
   x.tm.sync();
-  for (int j = x.tid; j < tc::kThetaWords / 2; j += x.nth) {
+  constexpr int kHalf = 64;
+  if (f16) {
+    float fmax = 0.f;
+    for (int k = x.tid; k < x.cfg.D; k += x.nth) fmax = fmaxf(fmax, fabsf(tc::theta_f32(rq[k])));
+    fmax = x.tm.max(fmax);
+    const int e = tc::theta_exp_f16(fmax);
+    const float scale = tc::exp2_int(-e);
+    for (int j = x.tid; j < kHalf; j += x.nth) {
+      const int k = 2 * j;
+      uint32_t wh, wl;
+      tc::theta_words_f16(k < x.cfg.D ? tc::theta_f32(rq[k]) : 0.f,
+                          k + 1 < x.cfg.D ? tc::theta_f32(rq[k + 1]) : 0.f, scale, wh, wl);
+      w[j] = wh;
+      w[kHalf + j] = wl;
+    }
+    if (x.tid == 0) w[tc::kThetaExpWord] = (uint32_t)e;
+    return;
+  }
+  for (int j = x.tid; j < kHalf; j += x.nth) {
     const int k = 2 * j;
     uint32_t wh, wl;
     tc::theta_words(k < x.cfg.D ? rq[k] : 0.0, k + 1 < x.cfg.D ? rq[k + 1] : 0.0, wh, wl);
     w[j] = wh;
-    w[tc::kThetaWords / 2 + j] = wl;
+    w[kHalf + j] = wl;
   }
 }
 
@@ -689,7 +712,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
           rq[i] = v;
         }
         if (!inits && cfg.init_radius != 0.0) st.nu += D;
-        if (req_tc) pack_request_words(x, rq, req_tc);
+        if (req_tc) pack_request_words(x, rq, req_tc, f.req_tc_f16);
         st.phase = PH_INIT_EVAL;
         yield = true;
         break;
@@ -746,7 +769,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         const double e = st.nom_eps;
         half_kick(x, p, g, 0.5 * e);
         drift_and_request(x, q, p, e, rq);
-        if (req_tc) pack_request_words(x, rq, req_tc);
+        if (req_tc) pack_request_words(x, rq, req_tc, f.req_tc_f16);
         st.phase = PH_SS_EVAL;
         yield = true;
         break;
@@ -887,7 +910,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         const double e = st.dir * st.eps;
         half_kick(x, p, g, 0.5 * e);
         drift_and_request(x, q, p, e, rq);
-        if (req_tc) pack_request_words(x, rq, req_tc);
+        if (req_tc) pack_request_words(x, rq, req_tc, f.req_tc_f16);
         st.phase = PH_LEAF_EVAL;
         yield = true;
         break;
@@ -1121,12 +1144,11 @@ void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* sta
   nuts_init_kernel<<<blocks, threads, 0, s>>>(cfg, states, stacks, vecs, inv_metrics, active);
 }
 
+static std::atomic<int> g_team_warps{0};
+void set_team_warps(int w) { g_team_warps.store((w == 1 || w == 2 || w == 4) ? w : 0); }
+
 int team_warps(int D) {
-  static const int forced = [] {
-    const char* e = getenv("GBNUTS_TEAM_WARPS");
-    const int w = e ? atoi(e) : 0;
-    return (w == 1 || w == 2 || w == 4) ? w : 0;
-  }();
+  const int forced = g_team_warps.load();
   if (forced) return forced;
   return D <= 64 ? 1 : (D <= 1024 ? 2 : 4);
 }

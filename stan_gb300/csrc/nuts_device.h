@@ -94,8 +94,10 @@ struct FitPtrs {
   int* done_count;
   const int* abort_flag;
   // the request also as chains-on-M tensor-core words (kThetaWords per chain),
-  // or null when the gradient form does not read them
+  // or null when the gradient form does not read them; req_tc_f16 selects
+  // the fp16 words with the chain's scale exponent (the f16x3 form)
   uint32_t* req_tc;
+  int req_tc_f16;
   // dense_e: per chain three D x D matrices, column-major (element (i, j) at
   // j * D + i): the inverse metric A, its Cholesky factor L (lower, A = L L^T)
   // and the Welford second-moment sums M2; null for diag_e
@@ -114,7 +116,7 @@ struct PoolFitDev {
 };
 
 // Warps per chain of the step kernel for a dimension D: 1, 2 or 4 (1 up to
-// D = 64, 2 up to 1024; GBNUTS_TEAM_WARPS overrides it, for tuning).
+// D = 64, 2 up to 1024; gbnuts_set_launch_shape overrides it, for tuning).
 int team_warps(int D);
 
 // One step of `total` chains: chain_map[g] = (table index, chain in fit); all

@@ -13,6 +13,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 
 namespace gbn {
@@ -33,12 +34,13 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
-// Instruction descriptor, kind::f16: BF16 x BF16 -> FP32, dense.
+// Instruction descriptor, kind::f16: BF16 x BF16 -> FP32 (or, with f16 set,
+// F16 x F16 -> FP32), dense.
 __host__ __device__ constexpr uint32_t make_idesc_bf16(int M, int N, int a_mn_major,
-                                                       int b_mn_major) {
-  return (1u << 4)                 // D format: F32
-         | (1u << 7)               // A format: BF16
-         | (1u << 10)              // B format: BF16
+                                                       int b_mn_major, bool f16 = false) {
+  return (1u << 4)                          // D format: F32
+         | ((f16 ? 0u : 1u) << 7)           // A format: BF16 (1) or F16 (0)
+         | ((f16 ? 0u : 1u) << 10)          // B format: BF16 (1) or F16 (0)
          | ((uint32_t)a_mn_major << 15) | ((uint32_t)b_mn_major << 16) |
          ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
@@ -287,13 +289,55 @@ __device__ __forceinline__ void theta_words(double d0, double d1, uint32_t& wh, 
   wh = *reinterpret_cast<const uint32_t*>(&hp);
   wl = *reinterpret_cast<const uint32_t*>(&lo);
 }
-// Words per chain: 64 hi then 64 lo (128 features).
-constexpr int kThetaWords = 128;
+// Words per chain: 64 hi then 64 lo (128 features), then the chain's scale
+// exponent (fp16 words only) and padding to a 16-byte multiple.
+constexpr int kThetaWords = 132;
+constexpr int kThetaExpWord = 128;
+
+// The fp16 form's per-chain scale: theta_k log2(e) 2^-e has its largest
+// magnitude in [2^13, 2^14), so the hi parts stay far inside the fp16 range
+// and the lo parts (about 2^-11 of hi) stay normal for the large components.
+// fmax: largest |fp32 theta_k| log2(e) of the chain.
+__host__ __device__ __forceinline__ int theta_exp_f16(float fmax) {
+  if (!(fmax > 0.f) || fmax > 3.0e38f) return 0;
+  int e = 0;
+  frexpf(fmax, &e);  // fmax = m 2^e, m in [0.5, 1)
+  e = e - 1 - 13;
+  return e < -100 ? -100 : (e > 100 ? 100 : e);
+}
+
+// 2^e as a float for |e| <= 126.
+__device__ __forceinline__ float exp2_int(int e) {
+  return __int_as_float((127 + e) << 23);
+}
+
+// fp32 theta (already times log2(e)) pairs -> fp16 hi / lo words at scale 2^-e.
+__device__ __forceinline__ void theta_words_f16(float f0, float f1, float scale, uint32_t& wh,
+                                                uint32_t& wl) {
+  f0 *= scale;
+  f1 *= scale;
+  const __half2 hp = __floats2half2_rn(f0, f1);
+  const float2 hf = __half22float2(hp);
+  const __half2 lo = __floats2half2_rn(f0 - hf.x, f1 - hf.y);
+  wh = *reinterpret_cast<const uint32_t*>(&hp);
+  wl = *reinterpret_cast<const uint32_t*>(&lo);
+}
+
+// fp32 value of a theta element as the word builders see it.
+__device__ __forceinline__ float theta_f32(double d) {
+  return dbl_to_flt_rz(d) * 1.44269504f;
+}
 
 // bf16 hi/lo split of a value: hi = bf16(v), lo = bf16(v - hi).
 __device__ __forceinline__ void split_bf16(float v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
   hi = __float2bfloat16_rn(v);
   lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+}
+
+// fp16 hi/lo split: hi = f16(v), lo = f16(v - hi) (22 significant bits).
+__device__ __forceinline__ void split_f16(float v, __half& hi, __half& lo) {
+  hi = __float2half_rn(v);
+  lo = __float2half_rn(v - __half2float(hi));
 }
 
 }  // namespace tc

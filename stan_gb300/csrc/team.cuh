@@ -37,6 +37,19 @@ struct Team {
     return s;
   }
 
+  // Largest value over the team (order-independent, so deterministic).
+  __device__ __forceinline__ float max(float v) const {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if (nw == 1) return v;
+    if ((t & 31) == 0) red[(t >> 5) * 8] = (double)v;
+    sync();
+    float m = v;
+    for (int w = 0; w < nw; ++w) m = fmaxf(m, (float)red[w * 8]);
+    sync();
+    return m;
+  }
+
   // Six sums with one pair of barriers (the U-turn dot products of a merge).
   __device__ __forceinline__ void sum6(double* v) const {
 #pragma unroll

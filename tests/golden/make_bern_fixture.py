@@ -38,4 +38,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_bern_fixture.py <stan-dev/stan source tree>")
+    main(sys.argv[1])

@@ -13,8 +13,9 @@ def test_sweep_picks_fastest_and_reports_failures(monkeypatch):
         def __init__(self, rc, out, err=""):
             self.returncode, self.stdout, self.stderr = rc, out, err
 
-    def fake_run(cmd, env, cwd, capture_output, text, timeout):
-        sr, tw = int(env["GBNUTS_SPLIT_ROWS"]), int(env["GBNUTS_TEAM_WARPS"])
+    def fake_run(cmd, cwd, capture_output, text, timeout):
+        sr = int(cmd[cmd.index("--split-rows") + 1])
+        tw = int(cmd[cmd.index("--team-warps") + 1])
         calls.append((sr, tw))
         assert "--child" in cmd
         if sr == 128 and tw == 4:

@@ -47,6 +47,33 @@ def test_timing_reductions_over_two_gloo_ranks():
     assert out == [(0, 2, 0, 2.5, 30.0), (1, 2, 1, 2.5, 30.0)]
 
 
+def _select_main(rank, preset, q):
+    os.environ.pop("CUDA_VISIBLE_DEVICES", None)
+    if preset is not None:
+        os.environ["CUDA_VISIBLE_DEVICES"] = preset
+    sys.path.insert(0, ROOT)
+    import bench
+    dev = bench.select_device(2, rank)
+    q.put((rank, dev, os.environ["CUDA_VISIBLE_DEVICES"]))
+
+
+@pytest.mark.parametrize("preset,expect", [(None, ["0", "1"]), ("4,5,6,7", ["4", "5"]),
+                                           ("GPU-a, GPU-b", ["GPU-a", "GPU-b"])])
+def test_each_rank_narrows_the_visible_devices_to_its_own(preset, expect):
+    """Two ranks: each ends with exactly one visible GPU, its local rank's
+    entry of a list the launcher already exported (or its local rank)."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_select_main, args=(r, preset, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert out == [(0, expect[0], expect[0]), (1, expect[1], expect[1])]
+
+
 def test_single_rank_reductions_are_identities():
     sys.path.insert(0, ROOT)
     import bench

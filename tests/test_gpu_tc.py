@@ -1,8 +1,9 @@
 """Tensor-core (tcgen05, bf16 hi/lo) gradient path.
 
 The probe pushes small-integer bf16 matrices through both contraction layouts
-the gradient uses (K-major X.Theta^T and MN-major X^T.R); with such inputs the
-fp32 results are exact, so they must equal NumPy's.  The bf16x3 gradient is
+the gradient uses (A operands in tensor memory; X read K-major for eta and
+MN-major for X^T.R); with such inputs the fp32 results are exact, so they must
+equal NumPy's.  The bf16x3 gradient is
 then checked against the FP64 oracle: lp within 1e-5 relative, gradient
 within 1e-4 relative in the 2-norm.
 """
@@ -18,28 +19,6 @@ pytestmark = pytest.mark.gpu
 
 def _bf16_bits(a):
     return (np.ascontiguousarray(a, dtype=np.float32).view(np.uint32) >> 16).astype(np.uint16)
-
-
-def test_descriptor_probe_exact():
-    from stan_gb300 import _lib
-    lib = _lib.load()
-    f = lib.gbnuts_tc_probe
-    u16 = ctypes.POINTER(ctypes.c_uint16)
-    fp = ctypes.POINTER(ctypes.c_float)
-    f.restype = ctypes.c_int
-    f.argtypes = [u16, u16, u16, fp, fp]
-    rng = np.random.default_rng(0)
-    A = rng.integers(-2, 3, size=(128, 128)).astype(np.float32)
-    B = rng.integers(-2, 3, size=(64, 128)).astype(np.float32)
-    R = rng.integers(-2, 3, size=(128, 64)).astype(np.float32)
-    a, b, r = _bf16_bits(A), _bf16_bits(B), _bf16_bits(R)
-    D1 = np.zeros((128, 64), dtype=np.float32)
-    D2 = np.zeros((128, 64), dtype=np.float32)
-    rc = f(a.ctypes.data_as(u16), b.ctypes.data_as(u16), r.ctypes.data_as(u16),
-           D1.ctypes.data_as(fp), D2.ctypes.data_as(fp))
-    assert rc == 0, _lib.last_error()
-    assert np.array_equal(D1, A @ B.T), "K-major contraction (X . Theta^T) differs"
-    assert np.array_equal(D2, A.T @ R), "MN-major contraction (X^T . R) differs"
 
 
 def test_tensor_memory_operand_probe_exact():
@@ -75,15 +54,17 @@ def test_tensor_memory_operand_probe_exact():
     assert np.array_equal(D2, R @ X), "MN-major B contraction differs"
 
 
-@pytest.mark.parametrize("kind", ["logistic", "logistic_100k", "poisson"])
-def test_bf16x3_gradient_matches_fp64_oracle(kind):
+@pytest.mark.parametrize("kind,precision", [("logistic", "bf16x3"), ("logistic_100k", "bf16x3"),
+                                            ("poisson", "bf16x3"), ("logistic", "f16x3"),
+                                            ("logistic_100k", "f16x3")])
+def test_split_gradient_matches_fp64_oracle(kind, precision):
     from stan_gb300 import Model
     ds = make_dataset(kind, small=True, seed=9)
     m = Model.from_dataset(ds)
     om = ds.oracle_model()
     C = 70  # two chain groups, the second partly empty
     th = np.random.default_rng(4).normal(size=(C, m.D)) * 0.3
-    lp, g = m.log_prob_grad_batch(th, "bf16x3")
+    lp, g = m.log_prob_grad_batch(th, precision)
     for c in range(C):
         lpo, go = om.log_prob_grad(th[c])
         assert abs(lp[c] - lpo) <= 1e-5 * abs(lpo), (c, lp[c], lpo)
@@ -109,20 +90,75 @@ def test_bf16x3_full_size_logistic():
     assert rel.max() <= 1e-4
 
 
-def test_bf16x3_posterior_matches_fp64_within_mcse():
-    """Mixed-precision sampling gives the FP64 posterior: means within 4 MCSE."""
-    from stan_gb300 import Model, analyze, sampler
-    ds = make_dataset("logistic", small=False, seed=2)   # N = 1000, K = 25
+@pytest.mark.parametrize("precision,bound", [("f16x3", 1e-4), ("bf16x3", 3e-4)])
+def test_split_gradient_at_posterior_draws(precision, bound):
+    """N = 100000, K = 100 at 64 posterior-region points (Laplace draws).
+    There the gradient is small against its 1e5 terms, so representation
+    error in eta shows most: the fp16 split (22-bit operands) holds 1e-4 of
+    the FP64 gradient's 2-norm with a wide margin; the bf16 split (16-bit
+    operands) sits near 2e-4 and is held to 3e-4.  log p within 1e-6."""
+    from stan_gb300 import Model
+    from tests.datasets import logistic_laplace_draws
+    ds = make_dataset("logistic_100k", small=False, seed=1)
+    m = Model.from_dataset(ds)
+    th = logistic_laplace_draws(ds, 64, seed=11)
+    lp64, g64 = m.log_prob_grad_batch(th, "fp64")
+    lp, g = m.log_prob_grad_batch(th, precision)
+    rel = np.linalg.norm(g - g64, axis=1) / np.linalg.norm(g64, axis=1)
+    assert rel.max() <= bound, rel.max()
+    assert np.max(np.abs(lp - lp64) / np.abs(lp64)) <= 1e-6
+    om = ds.oracle_model()
+    lpo, go = om.log_prob_grad(th[0])
+    assert abs(lp64[0] - lpo) <= 1e-12 * abs(lpo)
+    assert np.linalg.norm(g64[0] - go) <= 1e-12 * np.linalg.norm(go) * 1e3
+
+
+def _moments_within_mcse(r64, rmx, D):
+    """Posterior mean and sd of every parameter within 4 combined MCSE
+    (mcse.hpp:22-61 estimates for each run)."""
+    from stan_gb300 import analyze
+    d64 = r64.sampling_draws()[:, :, 7:]
+    dmx = rmx.sampling_draws()[:, :, 7:]
+    worst = 0.0
+    for j in range(D):
+        a, b = d64[:, :, j], dmx[:, :, j]
+        se_m = np.hypot(analyze.mcse_mean(a), analyze.mcse_mean(b))
+        se_s = np.hypot(analyze.mcse_sd(a), analyze.mcse_sd(b))
+        zm = abs(a.mean() - b.mean()) / se_m
+        zs = abs(a.std() - b.std()) / se_s
+        assert zm <= 4, ("mean", j, zm)
+        assert zs <= 4, ("sd", j, zs)
+        worst = max(worst, zm, zs)
+    return worst
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "f16x3"])
+def test_mixed_posterior_matches_fp64_within_mcse(precision):
+    """Mixed-precision sampling gives the FP64 posterior (N = 1000, K = 25)."""
+    from stan_gb300 import Model, sampler
+    ds = make_dataset("logistic", small=False, seed=2)
     m = Model.from_dataset(ds)
     kw = dict(num_chains=8, num_warmup=500, num_samples=1000, random_seed=3)
     r64 = sampler.run(m, precision="fp64", **kw)
-    rmx = sampler.run(m, precision="bf16x3", **kw)
+    rmx = sampler.run(m, precision=precision, **kw)
     assert np.all(r64.status == 0) and np.all(rmx.status == 0)
-    d64 = r64.sampling_draws()[:, :, 7:]
-    dmx = rmx.sampling_draws()[:, :, 7:]
-    for j in range(m.D):
-        se = np.hypot(analyze.mcse_mean(d64[:, :, j]), analyze.mcse_mean(dmx[:, :, j]))
-        assert abs(d64[:, :, j].mean() - dmx[:, :, j].mean()) <= 4 * se, j
+    _moments_within_mcse(r64, rmx, m.D)
+
+
+@pytest.mark.timeout(900)
+def test_f16x3_posterior_matches_fp64_within_mcse_benchmark_design():
+    """The benchmark's design (N = 1e5, K = 100, X fp32 standardised) with 128
+    chains of 150 warmup + 200 draws in each form: means and sds of all 101
+    parameters within 4 MCSE of the FP64 run (a shorter run than the
+    benchmark's, so the FP64 side fits in a test)."""
+    from stan_gb300 import Model, sampler
+    ds = make_dataset("logistic_100k", small=False, seed=1)
+    m = Model.from_dataset(ds)
+    kw = dict(num_chains=128, num_warmup=150, num_samples=200, random_seed=5, init_radius=2.0)
+    r64 = sampler.run(m, precision="fp64", **kw)
+    rmx = sampler.run(m, precision="f16x3", **kw)
+    assert np.all(r64.status == 0) and np.all(rmx.status == 0)
+    _moments_within_mcse(r64, rmx, m.D)
 
 
 def _errors(m, om, th, precision):

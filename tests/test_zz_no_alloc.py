@@ -5,9 +5,10 @@ memory is pre-reserved by their own pool, or they run under another
 framework's allocator lock).  gbnuts_log_prob_grad_batch_device_noalloc
 serves them from a fixed device array inside the library.  This file checks,
 through the C ABI, that it returns what the regular batched entry point
-returns, on two calls in a row (the array keeps the previous call's
-contents), for a GLM and for a hierarchical model (whose group sums must be
-cleared on every call), and that an oversized request is refused.  It is
+returns, bit for bit, on two calls in a row (the array keeps the previous
+call's contents), for a GLM and for a hierarchical model (whose group sums
+must be cleared on every call), on a stream the caller created with two
+models calling in turn, and that an oversized request is refused.  It is
 named so that pytest collects it last.
 """
 import ctypes
@@ -57,7 +58,7 @@ class _Dev:
             self.rt.cudaFree(p)
 
 
-def _both(model, theta, precision):
+def _both(model, theta, precision, stream=None):
     from stan_gb300 import _lib
     lib = _lib.load()
     dev = _Dev()
@@ -66,7 +67,7 @@ def _both(model, theta, precision):
     outs = []
     for fn in (lib.gbnuts_log_prob_grad_batch_device, lib.gbnuts_log_prob_grad_batch_device_noalloc):
         d_lp, d_g = dev.alloc(C * 8), dev.alloc(C * D * 8)
-        rc = fn(model.handle, C, d_th, d_lp, d_g, _lib.PRECISIONS[precision], None)
+        rc = fn(model.handle, C, d_th, d_lp, d_g, _lib.PRECISIONS[precision], stream)
         assert rc == 0, _lib.last_error()
         dev.sync()
         outs.append((dev.get(d_lp, (C,)), dev.get(d_g, (C, D))))
@@ -74,10 +75,11 @@ def _both(model, theta, precision):
     return outs
 
 
-@pytest.mark.parametrize("kind,precision,tol", [("logistic_100k", "fp64", 1e-12),
-                                                 ("hier_normal", "fp64", 1e-12),
-                                                 ("logistic", "fp32", 1e-6)])
-def test_no_alloc_matches_regular_entry_point_twice(kind, precision, tol):
+@pytest.mark.parametrize("kind,precision", [("logistic_100k", "fp64"), ("hier_normal", "fp64"),
+                                            ("logistic", "fp32")])
+def test_no_alloc_matches_regular_entry_point_twice(kind, precision):
+    """Both entry points run the same kernels with the same row splits, so
+    their results are equal bit for bit, in either precision."""
     from stan_gb300 import Model
     ds = make_dataset(kind, small=True, seed=12)
     m = Model.from_dataset(ds)
@@ -85,8 +87,33 @@ def test_no_alloc_matches_regular_entry_point_twice(kind, precision, tol):
     for call in range(2):  # the second call sees the first call's leftovers
         th = rng.normal(size=(48, m.D)) * 0.3
         (lp_a, g_a), (lp_b, g_b) = _both(m, th, precision)
-        assert np.all(np.abs(lp_b - lp_a) <= tol * np.abs(lp_a)), call
-        assert np.max(np.abs(g_b - g_a)) <= tol * np.max(np.abs(g_a)), call
+        assert np.array_equal(lp_b, lp_a), call
+        assert np.array_equal(g_b, g_a), call
+
+
+def test_no_alloc_on_a_caller_stream_with_two_models_in_turn():
+    """A stream the caller created, and two models of different families
+    calling in turn on it: each call clears and rewrites what it reads from
+    the shared array (split bounds, group sums), so the hierarchical model
+    after the GLM, and the GLM after it, still equal the regular entry point."""
+    from stan_gb300 import Model
+    rt = _Dev().rt
+    rt.cudaStreamCreate.argtypes = [ctypes.POINTER(ctypes.c_void_p)]
+    rt.cudaStreamDestroy.argtypes = [ctypes.c_void_p]
+    st = ctypes.c_void_p()
+    assert rt.cudaStreamCreate(ctypes.byref(st)) == 0
+    try:
+        glm = Model.from_dataset(make_dataset("logistic_100k", small=True, seed=5))
+        hier = Model.from_dataset(make_dataset("hier_normal", small=True, seed=6))
+        rng = np.random.default_rng(9)
+        for m in (glm, hier, glm, hier):
+            th = rng.normal(size=(16, m.D)) * 0.3
+            (lp_a, g_a), (lp_b, g_b) = _both(m, th, "fp64", st)
+            assert np.array_equal(lp_b, lp_a)
+            assert np.array_equal(g_b, g_a)
+    finally:
+        rt.cudaStreamSynchronize(st)
+        rt.cudaStreamDestroy(st)
 
 
 def test_no_alloc_refuses_oversized_requests():
