@@ -36,7 +36,12 @@ sys.path.insert(0, ROOT)
 # DRAM bytes (read + write) of one launch of the dominant gradient kernel,
 # from an ncu capture of `python bench.py --case grad --workload W --precision P`
 # (one launch, dram__bytes_read.sum + dram__bytes_write.sum).
-TRAFFIC = {}
+TRAFFIC = {
+    ("logistic_100k", "f16x3"): (5.70e7, "ncu --set full --clock-control none -k regex:glm_tct "
+                                         "-s 1 -c 1 on python bench.py --case grad "
+                                         "--workload logistic_100k --precision f16x3: "
+                                         "53.8 MB read + 3.2 MB written, full-size launch"),
+}
 
 WORKLOADS = {
     "logistic_100k": dict(kind="logistic_100k", chains=1024, warmup=500, samples=1000),

@@ -509,7 +509,8 @@ int launch_partials(const ModelDesc& m, int precision, const double* Q, int ldq,
     dispatch_x<double>(m, Q, ldq, C, active, ws, stream);
   } else if (precision == GBNUTS_PREC_FP32) {
     dispatch_x<float>(m, Q, ldq, C, active, ws, stream);
-  } else if (is_tensor_precision(precision) && m.tc_xt != nullptr) {
+  } else if (is_tensor_precision(precision) &&
+             (precision == GBNUTS_PREC_F16X3 ? m.tc_xt16 : m.tc_xt) != nullptr) {
     int rc = launch_tct(m, precision, Q, ldq, C, active, ws, stream);
     if (rc) return rc;
   } else if (is_tensor_precision(precision) && m.gx_h != nullptr) {
