@@ -283,6 +283,11 @@ def run_ours(args, ws, rank, gpu):
             out["config_d"] = config_d_leg()
         except Exception as e:  # reported, not fatal to the headline line
             out["config_d"] = {"error": repr(e)}
+    if rank == 0 and not args.no_config_a:
+        try:
+            out["config_a"] = config_a_leg()
+        except Exception as e:  # reported, not fatal to the headline line
+            out["config_a"] = {"error": repr(e)}
     if rank == 0 and not args.no_serving:
         try:
             out["serving"] = serving_leg()
@@ -409,10 +414,13 @@ def fp64_rate(model, ds, C):
             "sample": f"{C} chains x 20 warmup iterations", "grad_kernel_ms": res.grad_ms}
 
 
-SERVING = dict(fits=16, rate=2.0, chains=4, warmup=300, samples=500, steps_per_call=32)
+# The default serving leg: 100 fits at 1 fit/s, about 70 % of the mixed form's
+# measured capacity on this stream, so latency is service time, not a growing queue.
+SERVING = dict(fits=100, rate=1.0, chains=4, warmup=300, samples=500, steps_per_call=32,
+               forms=("fp32",))
 
 
-def serving_leg(n_fits=None, rate=None, forms=("fp32", "fp64")):
+def serving_leg(n_fits=None, rate=None, forms=None):
     """Continuous batching on the serving stream (N log-uniform in [200, 5e4],
     K in {8, ..., 128}, data at prior draws, 4 chains, 300 + 500): fits
     arrive as a Poisson process and run in one pool per form; p50 / p99
@@ -423,6 +431,7 @@ def serving_leg(n_fits=None, rate=None, forms=("fp32", "fp64")):
     from stan_gb300 import workloads
     from stan_gb300.serving import Pool, poisson_arrivals, serve
     S = SERVING
+    forms = forms or S["forms"]
     n_fits = n_fits or S["fits"]
     rate = rate or S["rate"]
     dss = workloads.serving_stream(n_fits)
@@ -455,6 +464,94 @@ def serving_leg(n_fits=None, rate=None, forms=("fp32", "fp64")):
         summ["max_rhat_max_over_fits"] = float(np.max(list(rhat.values())))
         out["mixed" if form == "fp32" else "fp64"] = summ
     return out
+
+
+def _moment_z(d_a, d_b):
+    """Largest |difference| / combined MCSE over parameters, of posterior means
+    and of posterior sds (mcse.hpp:22-61 estimates on each run's draws)."""
+    from stan_gb300 import analyze
+    zm, zs = 0.0, 0.0
+    for j in range(d_a.shape[2]):
+        a, b = d_a[:, :, j], d_b[:, :, j]
+        se_m = np.hypot(analyze.mcse_mean(a), analyze.mcse_mean(b))
+        se_s = np.hypot(analyze.mcse_sd(a), analyze.mcse_sd(b))
+        zm = max(zm, abs(a.mean() - b.mean()) / se_m)
+        zs = max(zs, abs(a.std() - b.std()) / se_s)
+    return zm, zs
+
+
+def fp64_fit_leg(chains=128, mixed="f16x3"):
+    """The plain FP64 form and the mixed form, each a complete fit of the
+    benchmark's design (N = 1e5, K = 100, 500 warmup + 1000 draws) with
+    `chains` chains: measured min bulk ESS/s (fit wall time on the device),
+    gradient evaluations/s, their ratio, and the posterior moments of the two
+    runs compared in MCSE units."""
+    from stan_gb300 import Model, sampler, workloads
+    ds = workloads.make_dataset("logistic_100k", seed=1)
+    m = Model.from_dataset(ds)
+    kw = dict(num_chains=chains, num_warmup=500, num_samples=1000, adapt=True, max_depth=10,
+              delta=0.8, init_radius=2.0, random_seed=4242)
+    out = {"workload": f"logistic GLM N={ds.N} K={ds.K} X fp32, {chains} chains, "
+                       "500 warmup + 1000 draws"}
+    draws = {}
+    for form in ("fp64", mixed):
+        res = sampler.run(m, precision=form, **kw)
+        g, sec, ess, which = fit_stats(res, ds)
+        out[form] = {"fit_seconds": sec, "grad_evals_per_s": g / sec, "min_bulk_ess": ess,
+                     "min_bulk_ess_per_s": ess / sec, "min_ess_param": which,
+                     "grad_kernel_ms": res.grad_ms, "status_ok": bool(np.all(res.status == 0))}
+        draws[form] = res.sampling_draws()[:, :, 7:]
+    out["mixed_over_fp64_min_bulk_ess_per_s"] = (out[mixed]["min_bulk_ess_per_s"] /
+                                                 out["fp64"]["min_bulk_ess_per_s"])
+    zm, zs = _moment_z(draws["fp64"], draws[mixed])
+    out["moments_max_z"] = {"mean": zm, "sd": zs, "bound": 4.0}
+    m.close()
+    return out
+
+
+def config_a_leg(reps=3):
+    """The drop-in case: logistic N = 1000, K = 25 (X fp64), 4 chains, 1000
+    warmup + 1000 draws, FP64, adaptive.  The GPU form through the array API
+    (device time, CUDA events) against the CPU restatement of the reference
+    sampler running the same 4 chains on 4 host threads (wall time); min bulk
+    ESS/s and gradient evaluations/s on both sides, and the GPU's time per
+    step (one step-kernel launch and one gradient launch; steps run in
+    captured CUDA-graph chunks)."""
+    import oracle
+    from stan_gb300 import Model, analyze, sampler, workloads
+    ds = workloads.make_dataset("logistic", seed=1)
+    m = Model.from_dataset(ds)
+    kw = dict(num_chains=4, num_warmup=1000, num_samples=1000, adapt=True, max_depth=10,
+              delta=0.8, init_radius=2.0)
+    sampler.run(m, precision="fp64", random_seed=1, **dict(kw, num_warmup=50, num_samples=10))
+    gpu = []
+    for i in range(reps):
+        res = sampler.run(m, precision="fp64", random_seed=100 + i, **kw)
+        g, sec, ess, _ = fit_stats(res, ds)
+        gpu.append({"fit_seconds": sec, "grad_evals_per_s": g / sec, "min_bulk_ess_per_s": ess / sec,
+                    "ms_per_step": res.total_ms / max(res.steps, 1), "steps": int(res.steps),
+                    "grad_kernel_ms": res.grad_ms})
+    om = oracle.OracleModel(ds.kind, ds.X, ds.y, hp=list(ds.hp), intercept=ds.intercept,
+                            compensated=False)
+    cpu = []
+    for i in range(reps):
+        t0 = time.perf_counter()
+        r = om.sample(seed=100 + i, num_threads=4, **{k: v for k, v in kw.items()
+                                                       if k != "num_chains"}, num_chains=4)
+        dt = time.perf_counter() - t0
+        rows = r["rows"][:, -1000:]
+        q = np.concatenate([rows[:, :, 0:1], rows[:, :, 7:]], axis=2).transpose(1, 0, 2)
+        ess, _ = analyze.min_bulk_ess(q)
+        cpu.append({"fit_seconds": dt, "grad_evals_per_s": float(r["n_grad_total"].sum()) / dt,
+                    "min_bulk_ess_per_s": ess / dt})
+    med = lambda rs, k: float(np.median([x[k] for x in rs]))  # noqa: E731
+    m.close()
+    return {"workload": "logistic GLM N=1000 K=25 X fp64, 4 chains, 1000 warmup + 1000 draws, "
+                        "FP64, adaptive",
+            "gpu_fp64": {k: med(gpu, k) for k in gpu[0]},
+            "cpu_reference_restatement": dict({k: med(cpu, k) for k in cpu[0]},
+                                              threads=4, cores=os.cpu_count()),
+            "reps": reps}
 
 
 def run_reference(args, ws, rank):
@@ -554,11 +651,14 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-config-d", action="store_true")
     ap.add_argument("--no-csv", action="store_true")
+    ap.add_argument("--no-config-a", action="store_true")
     ap.add_argument("--serving-fits", type=int, default=None)
     ap.add_argument("--serving-rate", type=float, default=None)
-    ap.add_argument("--serving-forms", default="fp32,fp64",
+    ap.add_argument("--serving-forms", default="fp32",
                     help="comma list of the serving leg's gradient forms (fp32: mixed)")
-    ap.add_argument("--case", default="fit", choices=["fit", "grad", "shortfit", "serving"],
+    ap.add_argument("--fp64-fit-chains", type=int, default=128)
+    ap.add_argument("--case", default="fit",
+                    choices=["fit", "grad", "shortfit", "serving", "fp64fit", "config_a"],
                     help="fit: the benchmark; grad: two batched-gradient launches of the "
                          "workload (for kernel captures); shortfit: a fit of --short-iters "
                          "warmup iterations (for launch lists)")
@@ -567,6 +667,12 @@ def main():
     if args.case == "serving":
         print(json.dumps(serving_leg(args.serving_fits, args.serving_rate,
                                      tuple(args.serving_forms.split(",")))))
+        return
+    if args.case == "fp64fit":
+        print(json.dumps(fp64_fit_leg(args.fp64_fit_chains)))
+        return
+    if args.case == "config_a":
+        print(json.dumps(config_a_leg()))
         return
     if args.case != "fit":
         profile_case(args)

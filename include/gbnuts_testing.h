@@ -17,6 +17,13 @@ extern "C" {
 int gbnuts_tct_probe(const uint32_t* Aw, const uint16_t* X, const uint32_t* Rw, float* D1,
                      float* D2);
 
+/* A bounded device wait made to run out: one thread waits on an mbarrier
+ * that nothing arrives on, with a limit of limit_cycles SM clock cycles (the
+ * library's kernels use about 2 s).  *code receives the error code the wait
+ * recorded (0 if it completed), *completed 1 if it completed.  Returns 0 when
+ * the launch ran and the device stayed usable. */
+int gbnuts_wait_probe(long long limit_cycles, int* code, int* completed);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgbnuts.so")
 SOURCES = ["loglik.cu", "nuts.cu", "capi.cu", "noalloc.cu", "pool.cu", "glm_tct.cu",
-           "glm_gemm.cu", "ess.cu", "csv.cpp"]
+           "glm_wide.cu", "ess.cu", "csv.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -61,7 +61,7 @@ def build(verbose=False, force=False):
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcublas", "-lcudart", "-lpthread"]
+    cmd = [nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -88,13 +88,15 @@ static int ensure_precision(gbnuts_model* m, int precision) {
     return GBNUTS_OK;
   }
   if (!tc_supported(m->desc) && tensor_form_supported(m->desc)) {
-    // wide design: bf16 copies of X for the GEMM form
-    if (m->d_gx_h) return GBNUTS_OK;
-    int rc = gemm_prepare(m->desc, &m->d_gx_h, &m->d_gx_l, m->stream);
+    // wide design: X as slab tiles for the cluster kernel
+    if (m->d_wide_xt) return GBNUTS_OK;
+    int tiles = 0;
+    int rc = wide_prepare(m->desc, &m->d_wide_xt, &m->d_tc_yt, &tiles, m->stream);
     if (rc) return rc;
     GBN_CUDA_TRY(cudaStreamSynchronize(m->stream));
-    m->desc.gx_h = m->d_gx_h;
-    m->desc.gx_l = m->d_gx_l;
+    m->desc.wide_xt = m->d_wide_xt;
+    m->desc.wide_tiles = tiles;
+    m->desc.tc_yt = m->d_tc_yt;
     return GBNUTS_OK;
   }
   if (!tc_supported(m->desc))
@@ -329,8 +331,7 @@ void gbnuts_model_destroy(gbnuts_model* m) {
   if (m->d_tc_xt) cudaFree(m->d_tc_xt);
   if (m->d_tc_xt16) cudaFree(m->d_tc_xt16);
   if (m->d_tc_yt) cudaFree(m->d_tc_yt);
-  if (m->d_gx_h) cudaFree(m->d_gx_h);
-  if (m->d_gx_l) cudaFree(m->d_gx_l);
+  if (m->d_wide_xt) cudaFree(m->d_wide_xt);
   if (m->d_theta) cudaFree(m->d_theta);
   if (m->d_X) cudaFree(m->d_X);
   if (m->d_y) cudaFree(m->d_y);

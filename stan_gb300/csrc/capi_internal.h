@@ -31,8 +31,7 @@ struct gbnuts_model {
   void* d_tc_xt = nullptr;
   void* d_tc_xt16 = nullptr;
   float* d_tc_yt = nullptr;
-  void* d_gx_h = nullptr;
-  void* d_gx_l = nullptr;
+  void* d_wide_xt = nullptr;
 };
 
 

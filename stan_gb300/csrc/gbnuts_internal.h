@@ -63,9 +63,9 @@ struct ModelDesc {
   int tc_x_exp;
   const float* tc_yt;
   int tc_tiles;
-  // wide-design tensor-core form: X as row-major bf16 hi (and lo) copies
-  const void* gx_h;
-  const void* gx_l;
+  // wide-design tensor-core form: X as [tile][slab] 128 x 128 bf16 blocks
+  const void* wide_xt;
+  int wide_tiles;
 };
 
 // Number of per-(split, chain) partial sums: lp, sum r, sum r z_g, sum e^2, beta[K].
@@ -79,7 +79,6 @@ struct GradWorkspace {
   long long* split_rows = nullptr;  // [S+1] device
   int* err = nullptr;               // device error flag of bounded waits
   int precision = -1;
-  void* gemm = nullptr;  // buffers of the wide-design tensor-core form
   // theta of the current request as tensor-core words, written by the step
   // kernel during a sampler run (null otherwise)
   const uint32_t* tc_words = nullptr;
@@ -170,11 +169,15 @@ inline bool tensor_form_supported(const ModelDesc& m) {
   return (m.link == LINK_LOGIT || m.link == LINK_POISSON_LOG) && m.off_z < 0;
 }
 inline bool is_tensor_precision(int p) { return p == 2 || p == 3 || p == 4; }
-// Wide-design form (glm_gemm.cu): bf16 GEMMs around a link kernel.
-int gemm_kpad(const ModelDesc& m);
-int gemm_prepare(const ModelDesc& m, void** xh, void** xl, cudaStream_t st);
-int launch_gemm(const ModelDesc& m, int precision, const double* Q, int ldq, int C,
+// Wide-design form (glm_wide.cu, K + intercept > 128): one thread-block
+// cluster of F CTAs per (row split, 128 chains), a 128-feature slab per CTA.
+// wide_slabs: F (2 or 4), 0 when the design is outside the form's range.
+// wide_splits: row splits S (the partials then hold S split rows, or 2 S
+// when X is not stored in bf16: hi and lo columns of the gradient).
+int wide_slabs(const ModelDesc& m);
+int wide_splits(const ModelDesc& m, int C);
+int wide_prepare(const ModelDesc& m, void** xt, float** yt, int* n_tiles, cudaStream_t st);
+int launch_wide(const ModelDesc& m, int precision, const double* Q, int ldq, int C,
                 const int* active, GradWorkspace& ws, cudaStream_t st);
-void gemm_free_work(GradWorkspace& ws);
 
 }  // namespace gbn

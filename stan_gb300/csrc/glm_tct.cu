@@ -724,7 +724,41 @@ __global__ void __launch_bounds__(128, 1)
   }
 }
 
+// A wait that nothing satisfies, bounded by `limit` cycles (test hook).
+__global__ void wait_probe_kernel(long long limit, int* err, int* completed) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+    *completed = tc::mbar_wait_limit(&bar, 0, limit, err, 77) ? 1 : 0;
+  }
+}
+
 }  // namespace gbn
+
+extern "C" int gbnuts_wait_probe(long long limit_cycles, int* code, int* completed) {
+  using namespace gbn;
+  if (limit_cycles <= 0 || limit_cycles > 8000000000LL || !code || !completed) {
+    set_last_error("wait probe: limit_cycles in (0, 8e9] and non-null outputs");
+    return GBNUTS_USAGE;
+  }
+  int* d = nullptr;
+  GBN_CUDA_TRY(cudaMalloc(&d, 2 * sizeof(int)));
+  GBN_CUDA_TRY(cudaMemset(d, 0, 2 * sizeof(int)));
+  wait_probe_kernel<<<1, 32>>>(limit_cycles, d, d + 1);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int h[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    set_last_error(std::string("wait probe: ") + cudaGetErrorString(e));
+    return GBNUTS_SOFTWARE;
+  }
+  *code = h[0];
+  *completed = h[1];
+  return GBNUTS_OK;
+}
 
 // Test hook (include/gbnuts_testing.h): runs the probe kernel on host arrays.
 extern "C" int gbnuts_tct_probe(const uint32_t* Aw, const uint16_t* X, const uint32_t* Rw,

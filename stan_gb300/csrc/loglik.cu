@@ -430,7 +430,8 @@ static long long split_rows_min() {
 
 int choose_splits(const ModelDesc& m, int C, int precision) {
   if (is_tensor_precision(precision)) {
-    if (!tc_supported(m)) return 1;  // wide-design GEMM form: one partial row per chain
+    if (!tc_supported(m))  // wide-design cluster form
+      return wide_splits(m, C) * (m.x_dtype == GBNUTS_BF16 ? 1 : 2);
     return tct_splits(m, C);
   }
   const int CB = block_chains(m.K, C);
@@ -495,7 +496,6 @@ int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int pre
 
 void free_workspace(GradWorkspace& ws) {
   if (ws.partial) cudaFree(ws.partial);
-  gemm_free_work(ws);
   ws = GradWorkspace();
 }
 
@@ -513,8 +513,8 @@ int launch_partials(const ModelDesc& m, int precision, const double* Q, int ldq,
              (precision == GBNUTS_PREC_F16X3 ? m.tc_xt16 : m.tc_xt) != nullptr) {
     int rc = launch_tct(m, precision, Q, ldq, C, active, ws, stream);
     if (rc) return rc;
-  } else if (is_tensor_precision(precision) && m.gx_h != nullptr) {
-    int rc = launch_gemm(m, precision, Q, ldq, C, active, ws, stream);
+  } else if (is_tensor_precision(precision) && m.wide_xt != nullptr) {
+    int rc = launch_wide(m, precision, Q, ldq, C, active, ws, stream);
     if (rc) return rc;
   } else {
     set_last_error("precision not available for this model");

@@ -66,17 +66,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Waits for the phase of the given parity; gives up after ~2 s of SM clock.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
-                                          int code) {
+// Waits for the phase of the given parity; gives up after `limit` SM clock
+// cycles, recording `code` in *err.
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t* bar, uint32_t parity, long long limit,
+                                                int* err, int code) {
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > 4000000000LL) {
+    if (clock64() - t0 > limit) {
       if (err) atomicCAS(err, 0, code);
       return false;
     }
   }
   return true;
+}
+
+// The kernels' bound: ~2 s of SM clock.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
+                                          int code) {
+  return mbar_wait_limit(bar, parity, 4000000000LL, err, code);
 }
 
 // Bounded wait that also gives up when another role has set the CTA's abort flag.

@@ -106,3 +106,70 @@ def test_write_run_after_array_run(tmp_path):
         a = (tmp_path / f"svc_{c + 1}.csv").read_text()
         b = (tmp_path / f"arr_{c + 1}.csv").read_text()
         assert _strip_timing(a) == _strip_timing(b), c
+
+
+def test_resume_service_given_stepsize_and_metric():
+    """hmc_nuts_diag_e (hmc_nuts_diag_e.hpp:48-315, run_sampler.hpp): no
+    adaptation, the given step size and inverse metric in every row and in
+    the adaptation block run_sampler still writes, and the same draws as the
+    array API's non-adaptive run with the same seed."""
+    from stan_gb300 import Model, sampler, services
+    from stan_gb300.callbacks import StreamWriter
+    ds = make_dataset("logistic", small=True, seed=4)
+    m = Model.from_dataset(ds)
+    C, D = 2, m.D
+    inv = np.linspace(0.5, 1.5, D)
+    sample = [StreamWriter(io.StringIO()) for _ in range(C)]
+    rc = services.hmc_nuts_diag_e(m, C, None, inv, 17, 1, 2.0, 50, 60, 1, False, 0, 0.25, 0.0,
+                                  10, sample_writer=sample)
+    assert rc == 0
+    ref = sampler.run(m, num_chains=C, adapt=False, num_warmup=50, num_samples=60,
+                      stepsize=0.25, random_seed=17, init_radius=2.0,
+                      inv_metrics=np.tile(inv, (C, 1)))
+    for c in range(C):
+        lines = sample[c].stream.getvalue().split("\n")
+        assert lines[1] == "# Adaptation terminated"
+        assert lines[2] == "# Step size = 0.25"
+        assert lines[3] == "# Diagonal elements of inverse mass matrix:"
+        got = np.array([float(v) for v in lines[4][2:].split(", ")])
+        assert np.allclose(got, inv, rtol=1e-6)
+        rows = np.array([[float(v) for v in ln.split(",")] for ln in lines[5:5 + 60]])
+        assert np.all(rows[:, 2] == 0.25)
+        assert np.allclose(rows, ref.draws[c, :60], rtol=1e-5, atol=1e-6)
+
+
+def test_interrupt_callback_stops_the_run():
+    """The interrupt callback is polled between steps; a true answer stops
+    every chain (generate_transitions.hpp:52, where the interface's interrupt
+    throws): the service returns SOFTWARE, logs "Sampling interrupted." and
+    the chains have written fewer rows than requested."""
+    from stan_gb300 import Model, _lib, services
+    from stan_gb300.callbacks import Logger, StreamWriter
+    ds = make_dataset("logistic_100k", small=True, seed=5)
+    m = Model.from_dataset(ds)
+    C = 2
+    polls = []
+
+    class Stop:
+        def __call__(self):
+            polls.append(1)
+            return len(polls) >= 3
+
+    class Record(Logger):
+        def __init__(self):
+            self.lines = []
+
+        def error(self, msg):
+            self.lines.append(msg)
+
+    log = Record()
+    sample = [StreamWriter(io.StringIO()) for _ in range(C)]
+    kw = dict(KW, num_warmup=2000, num_samples=2000)
+    rc = services.hmc_nuts_diag_e_adapt(m, C, sample_writer=sample, interrupt=Stop(),
+                                        logger=log, **kw)
+    assert rc == _lib.SOFTWARE
+    assert len(polls) >= 3
+    assert "Sampling interrupted." in log.lines
+    for w in sample:
+        rows = [ln for ln in w.stream.getvalue().split("\n") if ln and not ln.startswith(("#", "lp__"))]
+        assert len(rows) < 2000

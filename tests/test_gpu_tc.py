@@ -173,8 +173,10 @@ def _errors(m, om, th, precision):
 
 @pytest.mark.parametrize("case", ["poisson_k512_bf16x", "logistic_k200_f32x"])
 def test_wide_design_bf16_forms_match_fp64_oracle(case):
-    """K + intercept > 127: the bf16 GEMM form.  Split (bf16x3): lp within 1e-5,
-    gradient within 1e-4 of the FP64 oracle; plain bf16: within 2e-2."""
+    """K + intercept > 127: the thread-block-cluster kernel (a 128-feature slab
+    per CTA; X stored in fp32 runs as [hi | lo] features).  Split (bf16x3): lp
+    within 1e-5, gradient within 1e-4 of the FP64 oracle; plain bf16: within
+    2e-2."""
     from stan_gb300 import Model, workloads
     if case == "poisson_k512_bf16x":
         ds = workloads.poisson(4096, 512, seed=3, x_dtype="bf16")
