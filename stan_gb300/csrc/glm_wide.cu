@@ -10,19 +10,23 @@
 //
 //   GEMM1  eta_f^T (128 chains x 128 rows) = Theta_f . X_tile,f^T   (partial eta)
 //   send   the partial for the rows CTA d owns (128 / F rows each) into CTA
-//          d's shared memory (distributed shared memory stores)
+//          d's shared memory (distributed shared memory)
 //   link   CTA f sums the F partials of its rows (in rank order, so every
 //          row's eta is the same sum wherever it is computed), applies the
-//          link (lp terms in a compensated fp32 sum per chain, r = d lp / d eta)
+//          link (lp terms in a compensated fp32 sum per chain, r = d lp / d eta);
+//          all 16 epilogue warps share the block, 128 / (4 F) rows each
 //   share  r of its rows, as bf16 hi / lo, into every CTA's residual tile
 //          (an A operand in shared memory, chains x rows, K-major)
 //   GEMM2  G_f^T (128 chains x 128 feats) += R . X_tile,f             (A = R, smem)
 //
-// Everything crossing CTAs is ordered by mbarriers: a sender waits until the
-// destination has consumed the previous tile's data (a remote arrive, or the
-// destination's MMA commit multicast to the cluster), writes, fences and
-// arrives on the destination's barrier with release semantics at cluster
-// scope; the receiver waits with acquire semantics.  Every wait is bounded.
+// Data crossing CTAs moves with st.async, which completes its bytes on an
+// mbarrier of the destination CTA; the destination arms that barrier once per
+// tile with the byte count it expects and waits on it (acquire, cluster
+// scope).  A sender first waits until the destination has consumed the
+// previous tile's data: the destination's warps arrive remotely on the
+// sender's barrier after reading their partials, and the destination's MMA
+// commit (multicast to the whole cluster) marks its residual tile read.
+// Every wait is bounded.
 //
 // X is stored per (tile, slab) as one 128 x 128 bf16 block in the canonical
 // K-major core-matrix layout.  X stored in bf16 is exact; X stored in fp32 or
@@ -51,41 +55,62 @@
 #include "tc_common.cuh"
 
 namespace gbn {
-
 using namespace tc;
 
 namespace wide {
 
 constexpr int TM = 128;                 // rows per tile
 constexpr int TF = 128;                 // features per slab
+constexpr int F = 4;                    // slabs (CTAs per cluster); narrower designs pad
+constexpr int RB = TM / F;              // rows of a tile whose link a CTA computes
+constexpr int QR = RB / 4;              // of which each epilogue warp takes QR
 constexpr int NCH = 128;                // chains per cluster (TMEM lanes)
 constexpr int SLAB_BYTES = TM * TF * 2;
-constexpr int STAGE_BYTES = SLAB_BYTES + 1024;  // X slab tile, y (fp32 x 128, padded)
-constexpr int STAGES = 3;
+constexpr int STAGE_BYTES = SLAB_BYTES + 512;   // X slab tile, y (fp32 x 128)
+constexpr int STAGES = 2;
 constexpr int R_PART = NCH * TM * 2;    // one bf16 part of the residual tile
+constexpr int R_BLOCK = NCH * RB * 2;   // one CTA's rows of one part (contiguous)
+constexpr int ETA_SLOT = NCH * RB * 4;  // one source's partials for a CTA's rows
 constexpr int NUM_EPI_WARPS = 16;
 constexpr int THREADS = 64 + 32 * NUM_EPI_WARPS;
-constexpr int ETA_BYTES = 3 * NCH * 32 * 4;     // the larger of F = 4 (3 x 32 rows) and F = 2
 constexpr int SMEM_X = 0;
 constexpr int SMEM_R = SMEM_X + STAGES * STAGE_BYTES;
-constexpr int SMEM_ETA = SMEM_R + 2 * R_PART;
-constexpr int SMEM_LP = SMEM_ETA + ETA_BYTES;    // [4][NCH] doubles, then [NCH] doubles
-constexpr int SMEM_BAR = SMEM_LP + 5 * NCH * 8;
-constexpr int SMEM_TOTAL = SMEM_BAR + 512;
-constexpr int SMEM_ALLOC = SMEM_TOTAL + 1024;
+// partials of a CTA's RB rows: a slot holds [RB / 4][NCH][4] floats (four
+// rows of one chain per 16-byte chunk, chains adjacent: conflict-free 16-byte
+// accesses across a warp's lanes)
+constexpr int SMEM_ETA = SMEM_R + 2 * R_PART;               // incoming, F - 1 slots
+constexpr int SMEM_OUT = SMEM_ETA + (F - 1) * ETA_SLOT;     // outgoing staging, F - 1 slots
+constexpr int SMEM_BAR = SMEM_OUT + (F - 1) * ETA_SLOT;
+constexpr int SMEM_TOTAL = SMEM_BAR + 256;
+constexpr int SMEM_ALLOC = SMEM_TOTAL + 128;                // slack for 128-byte alignment
+// lp scratch after the last tile ([4][NCH] + [NCH] doubles), in the outgoing
+// staging buffer once every copy out of it has completed
+constexpr int SMEM_LP = SMEM_OUT;
 constexpr uint32_t COL_D1 = 0, COL_D2 = 128, COL_TH = 256, COL_TL = 320;
 constexpr double kLn2 = 0.69314718055994530942;
 
 // barrier slots
 enum {
-  B_XFULL = 0, B_XEMPTY = 3, B_D1FULL = 6, B_D1EMPTY = 7, B_THETA = 8, B_ETAIN = 9,
-  B_ETAFREE = 10,  // [4]: destination d has consumed this CTA's partial
-  B_RFREE = 14,    // [4]: CTA d's GEMM2 has read its residual tile
-  B_RFULL = 18, B_D2FULL = 19, B_COUNT = 20
+  B_XFULL = 0, B_XEMPTY = 2, B_D1FULL = 4, B_D1EMPTY = 5, B_THETA = 6, B_ETAIN = 7,
+  B_ETAFREE = 8,   // [F]: destination d has consumed this CTA's partials
+  B_RFREE = 12,    // [F]: CTA d's GEMM2 has read its residual tile
+  B_RFULL = 16, B_D2FULL = 17,
+  B_STAGED = 18,   // [F]: the 4 warps of sub s have staged their partials for CTA s
+  B_ROWN = 22,     // the 16 epilogue warps have written this CTA's residual rows
+  B_COUNT = 23
 };
 
 __device__ __forceinline__ uint64_t desc_rows(uint32_t part, int ks) {
   return make_desc(part + 256 * ks, 128, (TF / 8) * 128);
+}
+// The residual tile (A of GEMM2: chains x tile rows, K-major) with the rows
+// outermost: element (m, k) at (k/8) 2048 + (m/8) 128 + (m%8) 16 + (k%8) 2, so
+// each CTA's RB rows are one contiguous block of R_BLOCK bytes.
+__device__ __forceinline__ uint32_t r_off(int m, int k) {
+  return (uint32_t)((k >> 3) * 2048 + (m >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2);
+}
+__device__ __forceinline__ uint64_t desc_r(uint32_t part, int ks) {
+  return make_desc(part + 4096 * ks, 2048, 128);
 }
 __device__ __forceinline__ uint64_t desc_feats(uint32_t part, int ks) {
   return make_desc(part + 4096 * ks, (TF / 8) * 128, 128);
@@ -102,22 +127,41 @@ __device__ __forceinline__ uint32_t mapa(uint32_t saddr, uint32_t rank) {
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
   return r;
 }
-__device__ __forceinline__ void st_cluster_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c,
-                                              uint32_t d) {
-  asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b),
-               "r"(c), "r"(d)
-               : "memory");
+// 16 bytes into CTA-cluster shared memory; completes `bytes` on the mbarrier
+// at cluster address mbar (in the same CTA as addr).
+__device__ __forceinline__ void st_async_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c,
+                                            uint32_t d, uint32_t mbar) {
+  asm volatile(
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];"
+      ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d), "r"(mbar)
+      : "memory");
+}
+// Bulk copy of this CTA's shared memory into CTA-cluster shared memory,
+// completing `bytes` on the mbarrier at cluster address mbar (in the
+// destination CTA).  Addresses 16-byte aligned, size a multiple of 16.
+__device__ __forceinline__ void bulk_copy_s2c(uint32_t dst, uint32_t src, uint32_t bytes,
+                                              uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(dst), "r"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
+// 8 consecutive fp32 columns of this thread's TMEM lane (32x32b shape).
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ double ld_cluster_f64(uint32_t addr) {
   double d;
   asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(d) : "r"(addr) : "memory");
   return d;
-}
-// This thread's earlier distributed-shared-memory writes: visible to the
-// tensor core's (async proxy) reads and ordered before its later release.
-__device__ __forceinline__ void fence_remote_writes() {
-  asm volatile("fence.proxy.async.shared::cluster;" ::: "memory");
-  asm volatile("fence.acq_rel.cluster;" ::: "memory");
 }
 __device__ __forceinline__ void arrive_remote(uint32_t cluster_addr) {
   asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr)
@@ -196,14 +240,14 @@ struct WideArgs {
   int* err;
 };
 
-template <int LINK, int F, bool SPLIT>
+template <int LINK, bool SPLIT>
 __global__ void __launch_bounds__(wide::THREADS, 1) glm_wide_kernel(WideArgs a) {
   using namespace wide;
-  constexpr int RB = TM / F;            // rows of a tile whose link this CTA computes
-  constexpr int SUBS_PER_DEST = 4 / F;  // epilogue subs (32 rows each) per owned block
+  constexpr uint32_t ETA_TILE = (F - 1) * ETA_SLOT;                  // partials in per tile
+  constexpr uint32_t R_IN = (F - 1) * R_BLOCK * (SPLIT ? 2 : 1);    // residual bytes in per tile
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
   double* sLP = reinterpret_cast<double*>(sm + SMEM_LP);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + SMEM_BAR);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + SMEM_BAR + 8 * B_COUNT);
@@ -231,13 +275,17 @@ __global__ void __launch_bounds__(wide::THREADS, 1) glm_wide_kernel(WideArgs a) 
     mbar_init(&bars[B_D1FULL], 1);
     mbar_init(&bars[B_D1EMPTY], NUM_EPI_WARPS);
     mbar_init(&bars[B_THETA], NUM_EPI_WARPS);
-    mbar_init(&bars[B_ETAIN], (F - 1) * 4 * SUBS_PER_DEST);
-    for (int d = 0; d < 4; ++d) {
-      mbar_init(&bars[B_ETAFREE + d], 4 * SUBS_PER_DEST);
+    // armed once per tile with the bytes the other CTAs' copies bring
+    mbar_init(&bars[B_ETAIN], 1);
+    // the MMA thread's arm plus this CTA's own rows
+    mbar_init(&bars[B_RFULL], 2);
+    for (int d = 0; d < F; ++d) {
+      mbar_init(&bars[B_ETAFREE + d], NUM_EPI_WARPS);
       mbar_init(&bars[B_RFREE + d], 1);
     }
-    mbar_init(&bars[B_RFULL], F * 4 * SUBS_PER_DEST);
     mbar_init(&bars[B_D2FULL], 1);
+    for (int d = 0; d < F; ++d) mbar_init(&bars[B_STAGED + d], 4);
+    mbar_init(&bars[B_ROWN], NUM_EPI_WARPS);
     *abort_s = 0;
     fence_mbar_init();
   }
@@ -245,7 +293,7 @@ __global__ void __launch_bounds__(wide::THREADS, 1) glm_wide_kernel(WideArgs a) 
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
-  // every CTA's barriers exist before any remote arrive
+  // every CTA's barriers exist before any copy or remote arrive
   cluster_sync();
   const uint32_t tmem = *tmem_slot;
 
@@ -276,22 +324,23 @@ __global__ void __launch_bounds__(wide::THREADS, 1) glm_wide_kernel(WideArgs a) 
       const uint32_t id2 = make_idesc_bf16(NCH, TF, 0, 1);
       const uint32_t rh = sm_base + SMEM_R, rl = rh + R_PART;
       const uint16_t all = (uint16_t)((1u << F) - 1);
+      if (n > 0) mbar_arrive_expect_tx(&bars[B_RFULL], R_IN);
       bool ok = mbar_wait_abortable(&bars[B_THETA], 0, abort_s, a.err, 42);
       fence_after_sync();
       auto gemm2 = [&](int i) -> bool {
         if (!wait_cluster(&bars[B_RFULL], i & 1, abort_s, a.err, 43)) return false;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         fence_after_sync();
         const int st = i % STAGES;
         const uint32_t xs = sm_base + SMEM_X + st * STAGE_BYTES;
 #pragma unroll 1
         for (int ks = 0; ks < TM / 16; ++ks) {
           const uint64_t bx = desc_feats(xs, ks);
-          mma_bf16(tmem + COL_D2, desc_rows(rh, ks), bx, id2, (i > 0 || ks > 0) ? 1u : 0u);
-          if (SPLIT) mma_bf16(tmem + COL_D2, desc_rows(rl, ks), bx, id2, 1u);
+          mma_bf16(tmem + COL_D2, desc_r(rh, ks), bx, id2, (i > 0 || ks > 0) ? 1u : 0u);
+          if (SPLIT) mma_bf16(tmem + COL_D2, desc_r(rl, ks), bx, id2, 1u);
         }
         mma_commit_multicast(&bars[B_RFREE + rank], all);
         mma_commit(&bars[B_XEMPTY + st]);
+        if (i + 1 < n) mbar_arrive_expect_tx(&bars[B_RFULL], R_IN);
         return true;
       };
       for (int i = 0; i < n && ok; ++i) {
@@ -316,15 +365,17 @@ __global__ void __launch_bounds__(wide::THREADS, 1) glm_wide_kernel(WideArgs a) 
     }
     __syncwarp();
   } else {
-    // ---- epilogue: warp (q, sub) owns chains 32q.. (TMEM lane quarter q)
-    // and rows / features 32 sub .. 32 sub + 31
+    // ---- epilogue: warp (q, sub) owns chains 32q.. (TMEM lane quarter q).
+    // Sub s's eta partial columns 32 s .. are the rows of CTA s: staged and
+    // bulk-copied there (sub == rank: this CTA's own rows).  Every warp then
+    // computes the link of QR of this CTA's own rows.
     const int q = warp & 3;
     const int sub = (warp - 2) >> 2;
     const int c = 32 * q + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
-    const int dest = (32 * sub) / RB;       // CTA whose rows this sub's columns are
-    const bool owner = dest == (int)rank;   // this warp computes the link of its rows
-    const int row_in_block = 32 * sub - RB * dest;
+    const int own0 = RB * (int)rank + QR * sub;   // first own row (tile row index)
+    const int oslot = sub < (int)rank ? sub : sub - 1;       // outgoing staging slot
+    const int islot = (int)rank < sub ? (int)rank : (int)rank - 1;  // my slot at CTA sub
     {
       // log2(e) Theta_f of this chain -> TMEM (features 32 sub .. of the slab)
       const bool act = act_s[c] != 0;
@@ -352,55 +403,63 @@ __global__ void __launch_bounds__(wide::THREADS, 1) glm_wide_kernel(WideArgs a) 
     bool ok = true;
     for (int i = 0; i < n && ok; ++i) {
       const int st = i % STAGES;
+      if (warp == 2 && lane == 0) mbar_arrive_expect_tx(&bars[B_ETAIN], ETA_TILE);
       if (!warp_wait(&bars[B_D1FULL], i & 1, abort_s, a.err, 46)) {
         ok = false;
         break;
       }
       fence_after_sync();
-      float v[32];
+      float v[32], o[QR];
       tmem_ld32(lane_addr + COL_D1 + 32 * sub, v);
+      tmem_ld8(lane_addr + COL_D1 + own0, o);
       tmem_ld_wait();
       fence_before_sync();
       __syncwarp();
       if (lane == 0) mbar_arrive(&bars[B_D1EMPTY]);
-      if (!owner) {
-        // send the partial for CTA dest's rows
-        if (!warp_wait_cluster(&bars[B_ETAFREE + dest], (i & 1) ^ 1, abort_s, a.err, 47)) {
+      if (sub != (int)rank) {
+        // stage the partial for CTA sub's rows (the staging slot is free once
+        // CTA sub has consumed the previous tile), then one bulk copy
+        if (!warp_wait_cluster(&bars[B_ETAFREE + sub], (i & 1) ^ 1, abort_s, a.err, 47)) {
           ok = false;
           break;
         }
-        const int slot = (int)rank < dest ? (int)rank : (int)rank - 1;
-        const uint32_t local = sm_base + SMEM_ETA + (uint32_t)((slot * NCH + c) * RB + row_in_block) * 4;
-        const uint32_t remote = mapa(local, (uint32_t)dest);
+        float4* stg = reinterpret_cast<float4*>(sm + SMEM_OUT + oslot * ETA_SLOT) + c;
 #pragma unroll
         for (int j = 0; j < 32; j += 4)
-          st_cluster_v4(remote + 4 * j, __float_as_uint(v[j]), __float_as_uint(v[j + 1]),
-                        __float_as_uint(v[j + 2]), __float_as_uint(v[j + 3]));
-        fence_remote_writes();
+          stg[(j >> 2) * NCH] = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+        fence_proxy_async();
         __syncwarp();
-        if (lane == 0) arrive_remote(mapa(smem_u32(&bars[B_ETAIN]), (uint32_t)dest));
-        continue;
+        if (lane == 0) mbar_arrive(&bars[B_STAGED + sub]);
+        if (q == 0 && lane == 0) {
+          ok = mbar_wait_abortable(&bars[B_STAGED + sub], i & 1, abort_s, a.err, 52);
+          if (ok)
+            bulk_copy_s2c(mapa(sm_base + SMEM_ETA + (uint32_t)(islot * ETA_SLOT), (uint32_t)sub),
+                          sm_base + SMEM_OUT + (uint32_t)(oslot * ETA_SLOT), ETA_SLOT,
+                          mapa(smem_u32(&bars[B_ETAIN]), (uint32_t)sub));
+        }
+        ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
+        if (!ok) break;
       }
-      // ---- owner: sum the F partials of rows 32 sub .. (rank order), link
+      // ---- own rows: the F partials summed in rank order, then the link
       if (!warp_wait_cluster(&bars[B_ETAIN], i & 1, abort_s, a.err, 48)) {
         ok = false;
         break;
       }
-      float e2[32];
+      float e2[QR];
 #pragma unroll
-      for (int j = 0; j < 32; ++j) e2[j] = 0.f;
+      for (int j = 0; j < QR; ++j) e2[j] = 0.f;
 #pragma unroll
       for (int r = 0; r < F; ++r) {
         if (r == (int)rank) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) e2[j] += v[j];
+          for (int j = 0; j < QR; ++j) e2[j] += o[j];
         } else {
           const int slot = r < (int)rank ? r : r - 1;
-          const float* src = reinterpret_cast<const float*>(sm + SMEM_ETA) +
-                             (size_t)(slot * NCH + c) * RB + row_in_block;
+          const float4* src = reinterpret_cast<const float4*>(sm + SMEM_ETA + slot * ETA_SLOT) +
+                              (QR * sub / 4) * NCH + c;
 #pragma unroll
-          for (int j = 0; j < 32; j += 4) {
-            const float4 p = *reinterpret_cast<const float4*>(src + j);
+          for (int j = 0; j < QR; j += 4) {
+            const float4 p = src[(j >> 2) * NCH];
             e2[j] += p.x;
             e2[j + 1] += p.y;
             e2[j + 2] += p.z;
@@ -409,17 +468,16 @@ __global__ void __launch_bounds__(wide::THREADS, 1) glm_wide_kernel(WideArgs a) 
         }
       }
       __syncwarp();
-      if (lane == 0)
-        for (int r = 0; r < F; ++r)
-          if (r != (int)rank) arrive_remote(mapa(smem_u32(&bars[B_ETAFREE + rank]), (uint32_t)r));
+      if (lane < F && lane != (int)rank)
+        arrive_remote(mapa(smem_u32(&bars[B_ETAFREE + rank]), (uint32_t)lane));
       const float* ys =
-          reinterpret_cast<const float*>(sm + SMEM_X + st * STAGE_BYTES + SLAB_BYTES) + 32 * sub;
-      const long long row0 = (long long)(t_begin + i) * TM + 32 * sub;
-      const int nvalid = (int)max(0LL, min(32LL, a.N - row0));
+          reinterpret_cast<const float*>(sm + SMEM_X + st * STAGE_BYTES + SLAB_BYTES) + own0;
+      const long long row0 = (long long)(t_begin + i) * TM + own0;
+      const int nvalid = (int)max(0LL, min((long long)QR, a.N - row0));
       float pa = 0.f, pb = 0.f;
-      uint32_t wh[16], wl[16];
+      uint32_t wh[QR / 2], wl[QR / 2];
 #pragma unroll
-      for (int j = 0; j < 32; j += 2) {
+      for (int j = 0; j < QR; j += 2) {
         float res[2];
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
@@ -456,31 +514,48 @@ __global__ void __launch_bounds__(wide::THREADS, 1) glm_wide_kernel(WideArgs a) 
       }
       two_sum_add(sa, pa);
       if (LINK != LINK_LOGIT) two_sum_add(sb, pb);
-      // ---- residual rows 32 sub .. of chain c into every CTA's residual tile
-      // (K-major core matrices: 8 rows of the tile = one 16-byte chunk)
-      const uint32_t off0 = (uint32_t)((c >> 3) * 2048 + (c & 7) * 16);
-      for (int d = 0; d < F; ++d) {
-        if (!warp_wait_cluster(&bars[B_RFREE + d], (i & 1) ^ 1, abort_s, a.err, 50)) {
-          ok = false;
-          break;
+      // ---- residual rows own0 .. of chain c into this CTA's residual tile,
+      // once every CTA's GEMM2 of the previous tile is done (they read this
+      // CTA's block through the copies below); then one thread copies the
+      // block to the other CTAs
+      if (lane == 0)
+        for (int d = 0; d < F && ok; ++d)
+          ok = wait_cluster(&bars[B_RFREE + d], (i & 1) ^ 1, abort_s, a.err, 50);
+      ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
+      if (!ok) break;
+      const uint32_t off = r_off(c, own0);
+      *reinterpret_cast<uint4*>(sm + SMEM_R + off) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+      if (SPLIT)
+        *reinterpret_cast<uint4*>(sm + SMEM_R + R_PART + off) =
+            make_uint4(wl[0], wl[1], wl[2], wl[3]);
+      fence_proxy_async();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bars[B_ROWN]);
+      if (warp == 2 && lane == 0) {
+        ok = mbar_wait_abortable(&bars[B_ROWN], i & 1, abort_s, a.err, 53);
+        if (ok) {
+          mbar_arrive(&bars[B_RFULL]);
+          const uint32_t blk = (uint32_t)(rank * R_BLOCK);
+          for (int d = 0; d < F; ++d) {
+            if (d == (int)rank) continue;
+            const uint32_t rbar = mapa(smem_u32(&bars[B_RFULL]), (uint32_t)d);
+            const uint32_t dst = mapa(sm_base + SMEM_R, (uint32_t)d);
+            bulk_copy_s2c(dst + blk, sm_base + SMEM_R + blk, R_BLOCK, rbar);
+            if (SPLIT)
+              bulk_copy_s2c(dst + R_PART + blk, sm_base + SMEM_R + R_PART + blk, R_BLOCK, rbar);
+          }
         }
-        const uint32_t rh = mapa(sm_base + SMEM_R, (uint32_t)d);
-#pragma unroll
-        for (int g = 0; g < 4; ++g) {
-          const uint32_t off = off0 + (uint32_t)(((32 * sub + 8 * g) >> 3) * 128);
-          st_cluster_v4(rh + off, wh[4 * g], wh[4 * g + 1], wh[4 * g + 2], wh[4 * g + 3]);
-          if (SPLIT)
-            st_cluster_v4(rh + R_PART + off, wl[4 * g], wl[4 * g + 1], wl[4 * g + 2],
-                          wl[4 * g + 3]);
-        }
-        fence_remote_writes();
-        __syncwarp();
-        if (lane == 0) arrive_remote(mapa(smem_u32(&bars[B_RFULL]), (uint32_t)d));
       }
+      ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
     }
-    // per-chain lp of this warp's rows
-    if (owner) sLP[sub * NCH + c] = kLn2 * ((double)sa.x + (double)sa.y) - ((double)sb.x + (double)sb.y);
-    else sLP[sub * NCH + c] = 0.0;
+    // per-chain lp of this warp's rows, in the staging buffer once every
+    // copy out of it has completed (each destination has consumed the last
+    // tile's partials)
+    if (lane == 0 && n > 0)
+      for (int d = 0; d < F; ++d)
+        if (d != (int)rank) wait_cluster(&bars[B_ETAFREE + d], (n - 1) & 1, abort_s, a.err, 54);
+    __syncwarp();
+    sLP[sub * NCH + c] = kLn2 * ((double)sa.x + (double)sa.y) - ((double)sb.x + (double)sb.y);
     // gradient partials: features 32 sub .. of the slab
     if (ok && warp_wait(&bars[B_D2FULL], 0, abort_s, a.err, 51)) {
       fence_after_sync();
@@ -542,10 +617,8 @@ __global__ void __launch_bounds__(wide::THREADS, 1) glm_wide_kernel(WideArgs a) 
 int wide_slabs(const ModelDesc& m) {
   const int kx = m.K + m.has_base;
   const int kf = m.x_dtype == GBNUTS_BF16 ? kx : 2 * kx;
-  const int F = (kf + wide::TF - 1) / wide::TF;
-  if (F <= 1) return 0;  // the narrow kernel's range
-  if (F == 2) return 2;
-  if (F <= 4) return 4;
+  if (kf <= wide::TF) return 0;           // the narrow kernel's range
+  if (kf <= wide::F * wide::TF) return wide::F;  // narrower designs pad to F slabs
   return 0;
 }
 
@@ -625,32 +698,26 @@ int wide_prepare(const ModelDesc& m, void** xt, float** yt, int* n_tiles, cudaSt
 }
 
 namespace {
-template <int LINK, int F, bool SPLIT>
-const void* wide_kernel_ptr() {
-  return reinterpret_cast<const void*>(glm_wide_kernel<LINK, F, SPLIT>);
-}
-
 // Clusters of F CTAs that fit on the device at once (one CTA per SM).
-int max_clusters(int F) {
+int max_clusters() {
   int dev = 0;
   cudaGetDevice(&dev);
   static std::mutex mu;
-  static std::map<std::pair<int, int>, int> cache;
+  static std::map<int, int> cache;
   std::lock_guard<std::mutex> lk(mu);
-  auto it = cache.find({dev, F});
+  auto it = cache.find(dev);
   if (it != cache.end()) return it->second;
-  const void* k = F == 2 ? wide_kernel_ptr<LINK_LOGIT, 2, true>()
-                         : wide_kernel_ptr<LINK_LOGIT, 4, true>();
+  const void* k = reinterpret_cast<const void*>(glm_wide_kernel<LINK_LOGIT, true>);
   int n = 0;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, wide::SMEM_ALLOC) ==
       cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(F, 1, 1);
+    cfg.gridDim = dim3(wide::F, 1, 1);
     cfg.blockDim = dim3(wide::THREADS, 1, 1);
     cfg.dynamicSmemBytes = wide::SMEM_ALLOC;
     cudaLaunchAttribute attr;
     attr.id = cudaLaunchAttributeClusterDimension;
-    attr.val.clusterDim.x = F;
+    attr.val.clusterDim.x = wide::F;
     attr.val.clusterDim.y = 1;
     attr.val.clusterDim.z = 1;
     cfg.attrs = &attr;
@@ -658,8 +725,8 @@ int max_clusters(int F) {
     if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess) n = 0;
   }
   cudaGetLastError();
-  if (n <= 0) n = std::max(1, device_sm_count() / F);
-  cache[{dev, F}] = n;
+  if (n <= 0) n = std::max(1, device_sm_count() / wide::F);
+  cache[dev] = n;
   return n;
 }
 }  // namespace
@@ -669,15 +736,15 @@ int wide_splits(const ModelDesc& m, int C) {
   if (F == 0) return 1;
   const int groups = (C + wide::NCH - 1) / wide::NCH;
   const int tiles = (int)((m.N + wide::TM - 1) / wide::TM);
-  int S = std::max(1, max_clusters(F) / groups);
+  int S = std::max(1, max_clusters() / groups);
   S = std::min(S, std::max(1, tiles));
   return S;
 }
 
-template <int LINK, int F, bool SPLIT>
+template <int LINK, bool SPLIT>
 static int launch_wide_t(const WideArgs& a, int groups, cudaStream_t st) {
   using namespace wide;
-  int rc = ensure_smem(glm_wide_kernel<LINK, F, SPLIT>, SMEM_ALLOC);
+  int rc = ensure_smem(glm_wide_kernel<LINK, SPLIT>, SMEM_ALLOC);
   if (rc) return rc;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(F, a.S, groups);
@@ -691,7 +758,7 @@ static int launch_wide_t(const WideArgs& a, int groups, cudaStream_t st) {
   attr.val.clusterDim.z = 1;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  GBN_CUDA_TRY(cudaLaunchKernelEx(&cfg, glm_wide_kernel<LINK, F, SPLIT>, a));
+  GBN_CUDA_TRY(cudaLaunchKernelEx(&cfg, glm_wide_kernel<LINK, SPLIT>, a));
   return GBNUTS_OK;
 }
 
@@ -721,18 +788,12 @@ int launch_wide(const ModelDesc& m, int precision, const double* Q, int ldq, int
   a.err = ws.err;
   const int groups = (C + wide::NCH - 1) / wide::NCH;
   const bool split = precision == GBNUTS_PREC_BF16X3;
-  if (m.link == LINK_LOGIT) {
-    if (F == 2)
-      return split ? launch_wide_t<LINK_LOGIT, 2, true>(a, groups, st)
-                   : launch_wide_t<LINK_LOGIT, 2, false>(a, groups, st);
-    return split ? launch_wide_t<LINK_LOGIT, 4, true>(a, groups, st)
-                 : launch_wide_t<LINK_LOGIT, 4, false>(a, groups, st);
-  }
-  if (F == 2)
-    return split ? launch_wide_t<LINK_POISSON_LOG, 2, true>(a, groups, st)
-                 : launch_wide_t<LINK_POISSON_LOG, 2, false>(a, groups, st);
-  return split ? launch_wide_t<LINK_POISSON_LOG, 4, true>(a, groups, st)
-               : launch_wide_t<LINK_POISSON_LOG, 4, false>(a, groups, st);
+  if (m.link == LINK_LOGIT)
+    return split ? launch_wide_t<LINK_LOGIT, true>(a, groups, st)
+                 : launch_wide_t<LINK_LOGIT, false>(a, groups, st);
+  return split ? launch_wide_t<LINK_POISSON_LOG, true>(a, groups, st)
+               : launch_wide_t<LINK_POISSON_LOG, false>(a, groups, st);
 }
 
 }  // namespace gbn
+
