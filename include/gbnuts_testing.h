@@ -6,6 +6,8 @@
 #ifndef GBNUTS_TESTING_H
 #define GBNUTS_TESTING_H
 #include <stdint.h>
+
+#include "gbnuts.h"
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -16,6 +18,16 @@ extern "C" {
  * patterns); D1, D2 128x128 fp32 outputs.  Returns 0 on success. */
 int gbnuts_tct_probe(const uint32_t* Aw, const uint16_t* X, const uint32_t* Rw, float* D1,
                      float* D2);
+
+/* gbnuts_sample_run with every chain's draws taken from the given arrays
+ * instead of the counter-based stream: chain c's uniform #n is
+ * uniforms[c * n_per_chain + n] and its normal #n normals[c * n_per_chain + n]
+ * (NaN past the end), consumed in the sampler's order (initial values,
+ * momentum draws, tree directions and acceptances).  For replaying a
+ * transition whose draws are known. */
+int gbnuts_sample_run_scripted(gbnuts_model* m, const gbnuts_run_config* cfg,
+                               gbnuts_run_output* out, const double* uniforms,
+                               const double* normals, int n_per_chain);
 
 /* A bounded device wait made to run out: one thread waits on an mbarrier
  * that nothing arrives on, with a limit of limit_cycles SM clock cycles (the

@@ -82,6 +82,9 @@ def lib():
             ctypes.c_int, ctypes.c_int, dp, dp, ctypes.POINTER(ctypes.c_int),
             ctypes.c_char_p, ctypes.c_int]
         L.oracle_mock_scenario.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, ctypes.c_int]
+        L.oracle_transition_scripted.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_double,
+                                                 ctypes.c_int, dp, ctypes.c_int, dp,
+                                                 ctypes.c_int, dp]
         L.oracle_covar_adaptation.argtypes = [ctypes.c_uint] * 4 + [
             ctypes.c_int, ctypes.c_int, dp, dp, ctypes.POINTER(ctypes.c_int)]
         L.oracle_dense_metric.argtypes = [ctypes.c_int, dp, dp, dp, dp, ctypes.c_uint,
@@ -130,6 +133,27 @@ class OracleModel:
         lp = ctypes.c_double()
         lib().oracle_log_prob_grad(self._h, _dp(th), int(propto), int(jacobian), ctypes.byref(lp), _dp(g))
         return lp.value, g
+
+    def transition_scripted(self, q0, uniforms, normals, stepsize, max_depth=10,
+                            inv_metric=None):
+        """One base_nuts transition from q0 with the given draws (diag_e).
+        Returns dict(q, lp, accept_stat, depth, n_leapfrog, divergent, energy,
+        uniforms_used, normals_used)."""
+        D = self.D
+        q0 = np.ascontiguousarray(q0, dtype=np.float64)
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        z = np.ascontiguousarray(normals, dtype=np.float64)
+        im = None if inv_metric is None else np.ascontiguousarray(inv_metric, dtype=np.float64)
+        out = np.zeros(D + 8)
+        rc = lib().oracle_transition_scripted(self._h, _dp(q0), None if im is None else _dp(im),
+                                              stepsize, max_depth, _dp(u), u.size, _dp(z),
+                                              z.size, _dp(out))
+        if rc != 0:
+            raise RuntimeError("scripted draws exhausted")
+        return {"q": out[:D].copy(), "lp": out[D], "accept_stat": out[D + 1],
+                "depth": int(out[D + 2]), "n_leapfrog": int(out[D + 3]),
+                "divergent": bool(out[D + 4]), "energy": out[D + 5],
+                "uniforms_used": int(out[D + 6]), "normals_used": int(out[D + 7])}
 
     def write_array(self, theta):
         th = np.ascontiguousarray(theta, dtype=np.float64)

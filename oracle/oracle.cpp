@@ -1551,6 +1551,44 @@ int oracle_dense_metric(int d, const double* a, const double* p, double* T, doub
 // scenario 1: build_tree_test, 2: rho_aggregation_test, 3: divergence_test,
 // 4: transition (mock_nuts), 5: transition_egde_momenta (max_depth 2).
 // Uniform draws come from `uniforms`; results are written to out.
+// One base_nuts transition (base_nuts.hpp:78-204) of a diag_e sampler from q0
+// with scripted draws: uniforms and normals are consumed in the sampler's
+// order (sample_p's D normals, then the direction and acceptance uniforms).
+// out: q (D values), then lp, accept_stat, depth, n_leapfrog, divergent,
+// energy, uniforms used, normals used.  Returns 0, or -1 when the script ran
+// out.
+int oracle_transition_scripted(void* mp, const double* q0, const double* inv_metric,
+                               double stepsize, int max_depth, const double* uniforms, int nu,
+                               const double* normals, int nz, double* out) {
+  const Model& m = *static_cast<Model*>(mp);
+  const int D = m.D;
+  try {
+    ScriptedSource rng(uniforms, nu, normals, nz);
+    DiagEHamiltonian ham(m, D);
+    if (inv_metric) ham.inv_metric.assign(inv_metric, inv_metric + D);
+    ExplLeapfrog integ;
+    Nuts s(ham, integ, rng, D);
+    s.set_nominal_stepsize(stepsize);
+    s.set_stepsize_jitter(0);
+    s.set_max_depth(max_depth);
+    Sample init;
+    init.q.assign(q0, q0 + D);
+    Sample r = s.transition(init);
+    for (int i = 0; i < D; ++i) out[i] = r.q[i];
+    out[D] = r.log_prob;
+    out[D + 1] = r.accept_stat;
+    out[D + 2] = s.depth;
+    out[D + 3] = s.n_leapfrog;
+    out[D + 4] = s.divergent ? 1.0 : 0.0;
+    out[D + 5] = s.energy;
+    out[D + 6] = (double)rng.n_uniform;
+    out[D + 7] = (double)rng.n_normal;
+    return 0;
+  } catch (const std::exception&) {
+    return -1;
+  }
+}
+
 int oracle_mock_scenario(int scenario, const double* uniforms, int n_uniforms,
                          double* out, int out_cap) {
   try {

@@ -155,6 +155,14 @@ static int ensure_scratch(gbnuts_model* m, int C) {
   return GBNUTS_OK;
 }
 
+// Draws of the next gbnuts_sample_run on this thread, when a test sets them
+// (gbnuts_sample_run_scripted): num_chains x len uniforms and normals.
+static thread_local struct {
+  const double* u = nullptr;
+  const double* z = nullptr;
+  int len = 0;
+} g_draw_script;
+
 // Read-only view of a model for the no-allocation entry point (noalloc.cu).
 int gbnuts_internal_model_view(const gbnuts_model* m, gbn::ModelDesc* desc,
                                const int** group_off) {
@@ -165,6 +173,20 @@ int gbnuts_internal_model_view(const gbnuts_model* m, gbn::ModelDesc* desc,
 }
 
 extern "C" {
+
+int gbnuts_sample_run_scripted(gbnuts_model* m, const gbnuts_run_config* cfg,
+                               gbnuts_run_output* out, const double* uniforms,
+                               const double* normals, int n_per_chain) {
+  if (!uniforms || !normals || n_per_chain <= 0)
+    return fail(GBNUTS_USAGE, "scripted draws: uniforms, normals and a positive length");
+  g_draw_script.u = uniforms;
+  g_draw_script.z = normals;
+  g_draw_script.len = n_per_chain;
+  const int rc = gbnuts_sample_run(m, cfg, out, nullptr);
+  g_draw_script.len = 0;
+  g_draw_script.u = g_draw_script.z = nullptr;
+  return rc;
+}
 
 int gbnuts_set_launch_shape(long long split_rows_min, int team_warps) {
   if (split_rows_min < 0 || !(team_warps == 0 || team_warps == 1 || team_warps == 2 ||
@@ -584,6 +606,9 @@ int make_sampler_cfg(const gbnuts_model* m, const gbnuts_run_config* rc, int max
   cfg.init_radius = rc->init_radius;
   cfg.seed = rc->random_seed;
   cfg.init_chain_id = rc->init_chain_id;
+  cfg.script_u = nullptr;
+  cfg.script_z = nullptr;
+  cfg.script_len = 0;
   cfg.idx_tau = m->desc.idx_tau;
   cfg.idx_sigma = m->desc.idx_sigma;
   WindowParams wp = window_params(rc->num_warmup, rc->init_buffer, rc->term_buffer, rc->window);
@@ -639,6 +664,20 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
     GBN_CUDA_TRY(dr.alloc(&d_inits, (size_t)C * D));
     GBN_CUDA_TRY(cudaMemcpyAsync(d_inits, rc->inits, (size_t)C * D * sizeof(double),
                                  cudaMemcpyHostToDevice, st));
+  }
+  if (g_draw_script.len > 0) {
+    // scripted draws (test hook): every chain's uniform and normal streams
+    const size_t n = (size_t)C * g_draw_script.len;
+    double *d_su, *d_sz;
+    GBN_CUDA_TRY(dr.alloc(&d_su, n));
+    GBN_CUDA_TRY(dr.alloc(&d_sz, n));
+    GBN_CUDA_TRY(cudaMemcpyAsync(d_su, g_draw_script.u, n * sizeof(double),
+                                 cudaMemcpyHostToDevice, st));
+    GBN_CUDA_TRY(cudaMemcpyAsync(d_sz, g_draw_script.z, n * sizeof(double),
+                                 cudaMemcpyHostToDevice, st));
+    cfg.script_u = d_su;
+    cfg.script_z = d_sz;
+    cfg.script_len = g_draw_script.len;
   }
   if (rc->inv_metrics && !cfg.dense) {
     GBN_CUDA_TRY(dr.alloc(&d_invm, (size_t)C * D));

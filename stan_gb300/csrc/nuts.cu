@@ -137,9 +137,26 @@ static __device__ double kinetic(const Ctx& x, const double* p) {
   return 0.5 * x.tm.sum(s);
 }
 
+// Chain c's uniform and normal #n: the counter-based stream, or a scripted
+// one (test hook).
+static __device__ __forceinline__ double uniform_n(const SamplerCfg& cfg, int c,
+                                                   unsigned long long n) {
+  if (cfg.script_u)
+    return n < (unsigned long long)cfg.script_len ? cfg.script_u[(size_t)c * cfg.script_len + n]
+                                                  : __longlong_as_double(0x7ff8000000000000LL);
+  return gbds_uniform_at(cfg.seed, cfg.init_chain_id + (unsigned)c, n);
+}
+static __device__ __forceinline__ double normal_n(const SamplerCfg& cfg, int c,
+                                                  unsigned long long n) {
+  if (cfg.script_z)
+    return n < (unsigned long long)cfg.script_len ? cfg.script_z[(size_t)c * cfg.script_len + n]
+                                                  : __longlong_as_double(0x7ff8000000000000LL);
+  return gbds_normal_at(cfg.seed, cfg.init_chain_id + (unsigned)c, n);
+}
+
 static __device__ __forceinline__ double draw_uniform(const SamplerCfg& cfg, ChainState& st,
                                                       int c) {
-  return gbds_uniform_at(cfg.seed, cfg.init_chain_id + (unsigned)c, st.nu++);
+  return uniform_n(cfg, c, st.nu++);
 }
 
 // sample_p (diag_e_metric.hpp:44-50): p_i = n_i / sqrt(invM_i), D normals.
@@ -149,9 +166,8 @@ static __device__ void sample_p_dense(const Ctx& x, ChainState& st, double* p) {
   const int D = x.cfg.D;
   const double* __restrict__ L = x.dm + (size_t)D * D;
   double* r = x.slot(SL_MS3);
-  const unsigned chain = x.cfg.init_chain_id + (unsigned)x.c;
   x.tm.sync();
-  for (int i = x.tid; i < D; i += x.nth) r[i] = gbds_normal_at(x.cfg.seed, chain, st.nn + i);
+  for (int i = x.tid; i < D; i += x.nth) r[i] = normal_n(x.cfg, x.c, st.nn + i);
   st.nn += D;
   for (int j = D - 1; j >= 0; --j) {
     x.tm.sync();
@@ -167,9 +183,8 @@ static __device__ void sample_p(const Ctx& x, ChainState& st, double* p) {
     return;
   }
   const double* im = x.slot(SL_INVM);
-  const unsigned chain = x.cfg.init_chain_id + (unsigned)x.c;
   for (int i = x.tid; i < x.cfg.D; i += x.nth)
-    p[i] = DDIV(gbds_normal_at(x.cfg.seed, chain, st.nn + i), __dsqrt_rn(im[i]));
+    p[i] = DDIV(normal_n(x.cfg, x.c, st.nn + i), __dsqrt_rn(im[i]));
   st.nn += x.cfg.D;
 }
 
@@ -704,10 +719,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
           else if (cfg.init_radius == 0.0)
             v = 0.0;
           else
-            v = DMUL(DSUB(2.0 * gbds_uniform_at(cfg.seed, cfg.init_chain_id + (unsigned)c,
-                                                 st.nu + i),
-                          1.0),
-                     cfg.init_radius);
+            v = DMUL(DSUB(2.0 * uniform_n(cfg, c, st.nu + i), 1.0), cfg.init_radius);
           q[i] = v;
           rq[i] = v;
         }

@@ -45,6 +45,12 @@ struct SamplerCfg {
   unsigned seed, init_chain_id;
   int idx_tau, idx_sigma;
   int dense;  // 1: dense_e metric (FitPtrs::dense), 0: diag_e (slot SL_INVM)
+  // Test hook: when set, chain c's uniform #n is script_u[c * script_len + n]
+  // and its normal #n script_z[c * script_len + n] (NaN past the end) instead
+  // of the counter-based stream (device pointers; null in every other run).
+  const double* script_u;
+  const double* script_z;
+  int script_len;
 };
 
 struct ChainState {

@@ -22,6 +22,9 @@ def test_library_exports_every_declared_function():
     assert missing == []
     # the Python binding declares exactly the exported C ABI
     assert set(names) == set(_lib.SIGNATURES)
+    # the test hooks are exported too
+    hooks = declared_functions("gbnuts_testing.h")
+    assert hooks and [n for n in hooks if not hasattr(lib, n)] == []
 
 
 def test_library_is_in_tree():

@@ -108,3 +108,48 @@ def test_multi_warp_chains_replay(J):
     o = om.sample(seed=9, **kw)
     assert np.all(r.status == 0) and np.all(o["return_code"] == 0)
     _compare(r, o, 4)
+
+
+def test_device_reproduces_the_reference_golden_transition():
+    """unit_e_nuts_test.cpp:311-355 on the device: the gauss3D model (written
+    as a Poisson GLM whose single row, x = 0 and y = 0, adds the constant -1
+    to lp), one non-adaptive transition from q = (1, -1, 1) with step size
+    0.1 and the draws recovered from the reference's expected values
+    (tests/golden/gauss3d_transition.json).  The device's row must carry the
+    reference's depth, leapfrog count, draw, log_prob and accept_stat to
+    EXPECT_FLOAT_EQ precision (4 float ulps)."""
+    import ctypes
+    import json
+    import os
+
+    from stan_gb300 import Model, _lib, sampler
+    with open(os.path.join(os.path.dirname(__file__), "golden", "gauss3d_transition.json")) as f:
+        fx = json.load(f)
+    g = fx["golden"]
+    m = Model(2, np.zeros((1, 3)), np.zeros(1), hp=[1.0], intercept=False)
+    cfg, out, res = sampler.prepare(3, 1, adapt=False, num_warmup=0, num_samples=1,
+                                    stepsize=fx["stepsize"], stepsize_jitter=0.0, max_depth=10,
+                                    inits=np.array(fx["q0"]), inv_metrics=np.ones(3),
+                                    precision="fp64")
+    n = max(len(fx["uniforms"]), 3) + 8
+    u = np.full(n, np.nan)
+    u[:len(fx["uniforms"])] = fx["uniforms"]
+    z = np.full(n, np.nan)
+    z[:3] = fx["normals"]
+    lib = _lib.load()
+    f = lib.gbnuts_sample_run_scripted
+    f.restype = ctypes.c_int
+    dp = ctypes.POINTER(ctypes.c_double)
+    f.argtypes = [ctypes.c_void_p, ctypes.POINTER(_lib.RunConfig), ctypes.POINTER(_lib.RunOutput),
+                  dp, dp, ctypes.c_int]
+    rc = f(m.handle, ctypes.byref(cfg), ctypes.byref(out), u.ctypes.data_as(dp),
+           z.ctypes.data_as(dp), n)
+    assert rc == 0, _lib.last_error()
+    sampler.finish(out, res)
+    row = res.draws[0, 0]
+    ulp4 = lambda v: 4 * float(np.spacing(np.float32(abs(v))))  # noqa: E731
+    assert int(row[3]) == g["depth"] and int(row[4]) == g["n_leapfrog"] and row[5] == 0
+    for i in range(3):
+        assert abs(row[7 + i] - g["q"][i]) <= ulp4(g["q"][i]), (i, row[7 + i])
+    assert abs(row[0] + 1.0 - g["log_prob"]) <= ulp4(g["log_prob"]), row[0]
+    assert abs(row[1] - g["accept_stat"]) <= ulp4(g["accept_stat"]), row[1]
