@@ -441,7 +441,26 @@ int choose_splits(const ModelDesc& m, int C, int precision) {
   long long max_s = std::max(1LL, m.N / split_rows_min());
   int S = (int)std::min<long long>(max_s, std::max(1, (2 * sms + chain_blocks - 1) / chain_blocks));
   if (m.off_z >= 0) S = std::min(S, m.J);
-  return std::max(S, 1);
+  S = std::max(S, 1);
+  if (precision == GBNUTS_PREC_FP64 && m.off_z < 0) {
+    // The FP64 form's CTAs are long (the FP64 pipe) and, with a large tile,
+    // one fits per SM: a last wave that is mostly empty costs a whole CTA
+    // time.  Among S/2 .. 2S splits (the same minimum of rows each), take the
+    // one whose CTAs best fill whole waves, nearest to S on ties.
+    const size_t smem = partial_smem(m.K, C, partial_tile_rows(m.K, C, precision), precision);
+    const int per_sm = std::max(1, std::min(8, (int)((227u * 1024u) / std::max<size_t>(smem, 1))));
+    const long long slots = (long long)sms * per_sm;
+    auto fill = [&](int s) {
+      const long long ctas = (long long)s * chain_blocks;
+      return (double)ctas / (double)(((ctas + slots - 1) / slots) * slots);
+    };
+    int best = S;
+    for (int s = std::max(1, S / 2); s <= 2 * S && s <= max_s; ++s)
+      if (fill(s) > fill(best) + 1e-9 || (fill(s) > fill(best) - 1e-9 && abs(s - S) < abs(best - S)))
+        best = s;
+    S = best;
+  }
+  return S;
 }
 
 int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int precision,
