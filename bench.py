@@ -283,6 +283,11 @@ def run_ours(args, ws, rank, gpu):
             out["config_d"] = config_d_leg()
         except Exception as e:  # reported, not fatal to the headline line
             out["config_d"] = {"error": repr(e)}
+    if rank == 0 and not args.no_config_c:
+        try:
+            out["config_c"] = config_c_leg()
+        except Exception as e:  # reported, not fatal to the headline line
+            out["config_c"] = {"error": repr(e)}
     if rank == 0 and not args.no_config_a:
         try:
             out["config_a"] = config_a_leg()
@@ -509,6 +514,32 @@ def fp64_fit_leg(chains=128, mixed="f16x3"):
     return out
 
 
+def config_c_leg(precision="fp32"):
+    """Config C: non-centred hierarchical normal, J = 2000 groups (~42k rows),
+    K = 10, D = 2013, 256 chains, 500 warmup + 1000 draws, in the given form:
+    fit time, gradient evaluations/s, min bulk ESS/s, the gradient launch
+    time, and the form's errors against the FP64 GPU form at the chains'
+    final draws (lp, gradient 2-norm, |delta H| per chain)."""
+    from stan_gb300 import Model, sampler, workloads
+    ds = workloads.make_dataset("hier_normal", seed=1)
+    m = Model.from_dataset(ds)
+    kw = dict(num_chains=256, num_warmup=500, num_samples=1000, adapt=True, max_depth=10,
+              delta=0.8, init_radius=2.0)
+    sampler.run(m, precision=precision, random_seed=1, **dict(kw, num_warmup=20, num_samples=0))
+    res = sampler.run(m, precision=precision, random_seed=4321, **kw)
+    g, sec, ess, which = fit_stats(res, ds)
+    out = {"workload": f"hierarchical normal J={ds.J} (N={ds.N}) K={ds.K} D={m.D}, 256 chains, "
+                       "500 warmup + 1000 draws",
+           "precision": precision, "fit_seconds": sec, "grad_evals_per_s": g / sec,
+           "min_bulk_ess": ess, "min_bulk_ess_per_s": ess / sec, "min_ess_param": which,
+           "grad_kernel_ms": res.grad_ms, "ms_per_step": res.total_ms / max(res.steps, 1),
+           "status_ok": bool(np.all(res.status == 0))}
+    if precision != "fp64":
+        out["precision_errors"] = precision_errors(m, res, precision)
+    m.close()
+    return out
+
+
 def config_a_leg(reps=3):
     """The drop-in case: logistic N = 1000, K = 25 (X fp64), 4 chains, 1000
     warmup + 1000 draws, FP64, adaptive.  The GPU form through the array API
@@ -652,13 +683,15 @@ def main():
     ap.add_argument("--no-config-d", action="store_true")
     ap.add_argument("--no-csv", action="store_true")
     ap.add_argument("--no-config-a", action="store_true")
+    ap.add_argument("--no-config-c", action="store_true")
     ap.add_argument("--serving-fits", type=int, default=None)
     ap.add_argument("--serving-rate", type=float, default=None)
     ap.add_argument("--serving-forms", default="fp32",
                     help="comma list of the serving leg's gradient forms (fp32: mixed)")
     ap.add_argument("--fp64-fit-chains", type=int, default=128)
     ap.add_argument("--case", default="fit",
-                    choices=["fit", "grad", "shortfit", "serving", "fp64fit", "config_a"],
+                    choices=["fit", "grad", "shortfit", "serving", "fp64fit", "config_a",
+                             "config_c"],
                     help="fit: the benchmark; grad: two batched-gradient launches of the "
                          "workload (for kernel captures); shortfit: a fit of --short-iters "
                          "warmup iterations (for launch lists)")
@@ -673,6 +706,9 @@ def main():
         return
     if args.case == "config_a":
         print(json.dumps(config_a_leg()))
+        return
+    if args.case == "config_c":
+        print(json.dumps(config_c_leg(args.precision if args.precision != "f16x3" else "fp32")))
         return
     if args.case != "fit":
         profile_case(args)

@@ -171,7 +171,8 @@ def _errors(m, om, th, precision):
     return e_lp, e_g
 
 
-@pytest.mark.parametrize("case", ["poisson_k512_bf16x", "logistic_k200_f32x"])
+@pytest.mark.parametrize("case", ["poisson_k512_bf16x", "logistic_k200_f32x",
+                                  "logistic_k300_bf16x"])
 def test_wide_design_bf16_forms_match_fp64_oracle(case):
     """K + intercept > 127: the thread-block-cluster kernel (a 128-feature slab
     per CTA; X stored in fp32 runs as [hi | lo] features).  Split (bf16x3): lp
@@ -180,8 +181,10 @@ def test_wide_design_bf16_forms_match_fp64_oracle(case):
     from stan_gb300 import Model, workloads
     if case == "poisson_k512_bf16x":
         ds = workloads.poisson(4096, 512, seed=3, x_dtype="bf16")
-    else:
+    elif case == "logistic_k200_f32x":
         ds = workloads.logistic(3000, 200, seed=4, x_dtype="f32", standardise=True)
+    else:  # 301 features in 4 slabs (the last one partly padding), 2000 rows (a ragged tile)
+        ds = workloads.logistic(2000, 300, seed=5, x_dtype="bf16")
     m = Model.from_dataset(ds)
     om = ds.oracle_model()
     C = 130  # two chain blocks of 128, the second mostly empty
