@@ -718,16 +718,7 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   if (prc) return prc;
   prc = prepare_workspace(m->desc, m->h_group_off.data(), C, rc->precision, m->ws);
   if (prc) return prc;
-  // Tensor-core forms: a separate kernel sums each chain's split partials
-  // (in split order) after the gradient, so the step kernel's finalize reads
-  // one row per chain instead of one per split: the sum runs over every
-  // (chain, column) in parallel instead of inside each chain's serial step.
-  const bool reduce_splits = is_tensor_precision(rc->precision) && m->ws.S > 1;
-  double* d_psum = nullptr;
-  if (reduce_splits) GBN_CUDA_TRY(dr.alloc(&d_psum, (size_t)C * m->ws.NP));
-  const PartialsView pv = reduce_splits
-                              ? PartialsView{d_psum, m->ws.NP, 1, m->ws.gz}
-                              : PartialsView{m->ws.partial, m->ws.NP, m->ws.S, m->ws.gz};
+  const PartialsView pv{m->ws.partial, m->ws.NP, m->ws.S, m->ws.gz};
 
   int* h_done = nullptr;
   GBN_CUDA_TRY(cudaMallocHost(&h_done, sizeof(int)));
@@ -816,12 +807,9 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   // then the gradient stage writes split partials the next step finalises.
   auto enqueue_step = [&](cudaEvent_t e0, cudaEvent_t e1) -> int {
     launch_nuts_step_pool(d_fit, d_cmap, C, team_warps(D), st);
-    if (!pool_partials) {
-      const int r = launch_partials(m->desc, rc->precision, d_req, cfg.ld, C, d_active, m->ws,
-                                    st, e0, e1);
-      if (r || !reduce_splits) return r;
-      return launch_split_sums(m->ws.partial, m->ws.S, C, m->ws.NP, d_active, d_psum, st);
-    }
+    if (!pool_partials)
+      return launch_partials(m->desc, rc->precision, d_req, cfg.ld, C, d_active, m->ws, st, e0,
+                             e1);
     if (m->desc.off_z >= 0)
       GBN_CUDA_TRY(cudaMemsetAsync(m->ws.gz, 0, (size_t)C * m->desc.J * sizeof(double), st));
     if (e0) cudaEventRecord(e0, st);
@@ -841,7 +829,7 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   // upper bound on steps: every transition is at most 2^max_depth - 1 leapfrogs,
   // step-size searches are bounded by the 1e7 / 0 stops, 100 init tries.
   const long long max_steps = (iters + 2) * ((1LL << max_depth) + 200) + 1000;
-  const int launches_per_step = 2 + (m->desc.off_z >= 0 ? 1 : 0) + (reduce_splits ? 1 : 0);
+  const int launches_per_step = 2 + (m->desc.off_z >= 0 ? 1 : 0);
   int status_rc = GBNUTS_OK;
   long long launches = 0;
   for (long long chunk_i = 0;; ++chunk_i) {

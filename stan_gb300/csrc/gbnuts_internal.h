@@ -102,11 +102,6 @@ int launch_partials(const ModelDesc& m, int precision, const double* Q, int ldq,
                     const int* active, GradWorkspace& ws, cudaStream_t stream, cudaEvent_t ev0,
                     cudaEvent_t ev1);
 
-// out[c][k] = sum over s < S of P[s][c][k], added in split order, for the
-// active chains (active may be null): a chain's partials as one row.
-int launch_split_sums(const double* P, int S, int C, int NP, const int* active, double* out,
-                      cudaStream_t stream);
-
 // lp[C] and grad[C][ldg] of C chains at Q[C][ldq] (device pointers), with
 // Stan's propto/jacobian semantics; active (may be null) masks chains.
 int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int ldq,

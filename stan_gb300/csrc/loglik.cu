@@ -544,30 +544,6 @@ int launch_partials(const ModelDesc& m, int precision, const double* Q, int ldq,
   return GBNUTS_OK;
 }
 
-__global__ void __launch_bounds__(256) split_sums_kernel(const double* __restrict__ P, int S,
-                                                         int C, int NP,
-                                                         const int* __restrict__ active,
-                                                         double* __restrict__ out) {
-  const long long total = (long long)C * NP;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i / NP);
-    if (active && !active[c]) continue;
-    double a = 0.0;
-    for (int s = 0; s < S; ++s) a += P[(size_t)s * total + i];
-    out[i] = a;
-  }
-}
-
-int launch_split_sums(const double* P, int S, int C, int NP, const int* active, double* out,
-                      cudaStream_t stream) {
-  const long long total = (long long)C * NP;
-  const int blocks = (int)std::min<long long>((total + 255) / 256, 8LL * device_sm_count());
-  split_sums_kernel<<<blocks, 256, 0, stream>>>(P, S, C, NP, active, out);
-  GBN_CUDA_TRY(cudaGetLastError());
-  return GBNUTS_OK;
-}
-
 int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int ldq,
                          int C, const int* active, double* lp, double* grad, int ldg,
                          int propto, int jacobian, GradWorkspace& ws,
