@@ -222,6 +222,21 @@ GBDS_FN void gbds_sincos_2pi(double v, double* sn, double* cs) {
   }
 }
 
+/* Both normals of Box-Muller block b, #2b (cosine) and #2b+1 (sine), with
+ * the operations of gbds_normal_at: the same two values, from one
+ * logarithm and one sine/cosine evaluation. */
+GBDS_FN void gbds_normal_pair_at(uint32_t seed, uint32_t chain, uint64_t block, double* z_even,
+                                 double* z_odd) {
+  gbds_block b = gbds_block_at(seed, chain, GBDS_STREAM_NORMAL, block);
+  double u = gbds_u01(b.w[0], b.w[1]);
+  double v = gbds_u01(b.w[2], b.w[3]);
+  double r = GBDS_SQRT(GBDS_MUL(-2.0, gbds_ln(GBDS_SUB(1.0, u))));
+  double sn, cs;
+  gbds_sincos_2pi(v, &sn, &cs);
+  *z_even = GBDS_MUL(r, cs);
+  *z_odd = GBDS_MUL(r, sn);
+}
+
 GBDS_FN double gbds_normal_at(uint32_t seed, uint32_t chain, uint64_t n) {
   gbds_block b = gbds_block_at(seed, chain, GBDS_STREAM_NORMAL, n >> 1);
   double u = gbds_u01(b.w[0], b.w[1]);

@@ -1342,11 +1342,20 @@ int oracle_write_array(void* mp, const double* th, double* out) {
   return 0;
 }
 
+// stream 0: uniforms, 1: normals one at a time, 2: the same normals from
+// gbds_normal_pair_at (the pairwise form the GPU sampler draws momenta with).
 void oracle_draws(unsigned seed, unsigned chain, int stream, unsigned long long start,
                   int n, double* out) {
-  for (int i = 0; i < n; ++i)
-    out[i] = stream == 0 ? gbds_uniform_at(seed, chain, start + i)
-                         : gbds_normal_at(seed, chain, start + i);
+  for (int i = 0; i < n; ++i) {
+    if (stream == 2) {
+      double ze, zo;
+      gbds_normal_pair_at(seed, chain, (start + i) >> 1, &ze, &zo);
+      out[i] = ((start + i) & 1u) ? zo : ze;
+    } else {
+      out[i] = stream == 0 ? gbds_uniform_at(seed, chain, start + i)
+                           : gbds_normal_at(seed, chain, start + i);
+    }
+  }
 }
 
 void oracle_philox(const unsigned* ctr, const unsigned* key, unsigned* out) {

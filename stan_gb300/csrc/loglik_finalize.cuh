@@ -23,12 +23,38 @@ static constexpr int kLanesOverSplits = 32;
 
 // Column sums over the S splits of one chain's partials (row stride pstride)
 // into cs[k], k < NP.  With many splits: lanes over splits and a fixed
-// butterfly per column.  Otherwise lanes over columns, adding the splits in
-// split order, their loads issued eight at a time.  The order of additions
-// depends on S and NP only.
+// butterfly per column.  Otherwise lanes over columns (or column pairs, as
+// 16-byte loads, when the rows are 16-byte aligned), adding the splits in
+// split order, their loads issued ten (eight) at a time.  The order of
+// additions depends on S and NP only.
 __device__ __forceinline__ void split_column_sums(const double* __restrict__ Pc, size_t pstride,
                                                   int S, int NP, double* cs, const Team& tm) {
-  if (S >= kLanesOverSplits) {
+  if (S < kLanesOverSplits && ((NP | (int)(pstride & 1)) & 1) == 0 &&
+      (reinterpret_cast<uintptr_t>(Pc) & 15) == 0) {
+    const int npair = NP >> 1;
+    const size_t ps2 = pstride >> 1;
+    for (int jb = 0; jb < npair; jb += tm.n) {
+      const int j = jb + tm.t;
+      if (j < npair) {
+        const double2* __restrict__ src = reinterpret_cast<const double2*>(Pc) + j;
+        double a0 = 0, a1 = 0;
+        for (int s0 = 0; s0 < S; s0 += 10) {
+          double2 t[10];
+#pragma unroll
+          for (int u = 0; u < 10; ++u)
+            t[u] = (s0 + u < S) ? src[(size_t)(s0 + u) * ps2] : make_double2(0.0, 0.0);
+#pragma unroll
+          for (int u = 0; u < 10; ++u)
+            if (s0 + u < S) {
+              a0 += t[u].x;
+              a1 += t[u].y;
+            }
+        }
+        cs[2 * j] = a0;
+        cs[2 * j + 1] = a1;
+      }
+    }
+  } else if (S >= kLanesOverSplits) {
     // each warp of the team takes every nw-th column
     const int lane = tm.t & 31;
 #pragma unroll 4

@@ -24,6 +24,7 @@ enum Slot {
   SL_PFF, SL_PFB, SL_PBF, SL_PBB,
   SL_RHO, SL_INVM, SL_WM, SL_WM2,
   SL_MS0, SL_MS1, SL_MS2, SL_MS3,
+  SL_ZNEXT,  // the normals of the next momentum draw, when ChainState::z_ready
   SL_STACK
 };
 
@@ -66,6 +67,12 @@ struct ChainState {
   unsigned wa_num_warmup, wa_init_buffer, wa_term_buffer, wa_base_window;
   unsigned wa_counter, wa_next, wa_size;
   double w_n;
+  // Work drawn ahead in a short step, off the long path that ends one
+  // transition and begins the next: z_ready = the next D normals of the
+  // stream (from #nn) are in slot SL_ZNEXT; sa_pre_ready = sqrt and
+  // pow(-kappa) of sa_counter + 1 for the next learn_stepsize.
+  int z_ready, sa_pre_ready;
+  double sa_pre_sqrt, sa_pre_xeta;
 };
 
 // Per-level data of the pending left siblings (log sum weight, V of the

@@ -48,6 +48,15 @@ def test_uniform_stream_matches_numpy_restatement():
         assert u[n] == m * 2.0 ** -53
 
 
+def test_normal_pairs_equal_single_normals():
+    # the GPU sampler draws momenta a Box-Muller pair at a time
+    # (gbds_normal_pair_at); every value must equal gbds_normal_at's, bit for bit
+    for seed, chain, start in [(99, 3, 0), (1, 0, 7), (2 ** 31 + 5, 1023, 10 ** 9 + 1)]:
+        a = oracle.draws(seed, chain, 1, start, 257)
+        b = oracle.draws(seed, chain, 2, start, 257)
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
 def test_normal_stream_moments_and_box_muller():
     z = oracle.draws(99, 3, 1, 0, 400000)
     assert abs(z.mean()) < 5 / math.sqrt(z.size)
