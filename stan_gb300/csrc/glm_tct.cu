@@ -262,14 +262,20 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
           fence_after_sync();
           const int st = i % STAGES;
           const uint32_t xh = smem_u32(sm + SMEM_X + st * STAGE_BYTES);
-          const uint32_t xl = xh + PART_BYTES;
-#pragma unroll 1
-          for (int ks = 0; ks < TM / 16; ++ks) {
-            const uint64_t bh = desc_feats(xh, ks);
-            mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RH + 8 * ks, bh, id2,
-                            (i > 0 || ks > 0) ? 1u : 0u);
-            if (SPLIT) mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RL + 8 * ks, bh, id2, 1u);
-            if (kXlo) mma_bf16_tmem_a(tmem + COL_D2, tmem + COL_RH + 8 * ks, desc_feats(xl, ks), id2, 1u);
+          // descriptors advance by their start-address field (16-byte units);
+          // few instructions per MMA, as the issuing warp shares its
+          // scheduler with four epilogue warps
+          const uint64_t bh0 = desc_feats(xh, 0), bl0 = desc_feats(xh + PART_BYTES, 0);
+          const uint32_t drow = tmem + COL_D2, arh = tmem + COL_RH, arl = tmem + COL_RL;
+          mma_bf16_tmem_a(drow, arh, bh0, id2, i > 0 ? 1u : 0u);
+          if (SPLIT) mma_bf16_tmem_a(drow, arl, bh0, id2, 1u);
+          if (kXlo) mma_bf16_tmem_a(drow, arh, bl0, id2, 1u);
+#pragma unroll
+          for (int ks = 1; ks < TM / 16; ++ks) {
+            const uint64_t bh = bh0 + (uint64_t)(256 * ks);
+            mma_bf16_tmem_a(drow, arh + 8 * ks, bh, id2, 1u);
+            if (SPLIT) mma_bf16_tmem_a(drow, arl + 8 * ks, bh, id2, 1u);
+            if (kXlo) mma_bf16_tmem_a(drow, arh + 8 * ks, bl0 + (uint64_t)(256 * ks), id2, 1u);
           }
           mma_commit(&bars[B_REMPTY]);
           mma_commit(&bars[B_XEMPTY + st]);
@@ -282,13 +288,17 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
           if (!ok) break;
           fence_after_sync();
           const uint32_t xh = smem_u32(sm + SMEM_X + st * STAGE_BYTES);
-          const uint32_t xl = xh + PART_BYTES;
+          const uint64_t bh0 = desc_rows(xh, 0), bl0 = desc_rows(xh + PART_BYTES, 0);
+          const uint32_t d1 = tmem + COL_D1, ath = tmem + COL_TH, atl = tmem + COL_TL;
+          mma_bf16_tmem_a(d1, ath, bh0, id1, 0u);
+          if (SPLIT) mma_bf16_tmem_a(d1, atl, bh0, id1, 1u);
+          if (kXlo) mma_bf16_tmem_a(d1, ath, bl0, id1, 1u);
 #pragma unroll 1
-          for (int ks = 0; ks < ksteps; ++ks) {
-            const uint64_t bh = desc_rows(xh, ks);
-            mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TH + 8 * ks, bh, id1, ks > 0 ? 1u : 0u);
-            if (SPLIT) mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TL + 8 * ks, bh, id1, 1u);
-            if (kXlo) mma_bf16_tmem_a(tmem + COL_D1, tmem + COL_TH + 8 * ks, desc_rows(xl, ks), id1, 1u);
+          for (int ks = 1; ks < ksteps; ++ks) {
+            const uint64_t bh = bh0 + (uint64_t)(16 * ks);
+            mma_bf16_tmem_a(d1, ath + 8 * ks, bh, id1, 1u);
+            if (SPLIT) mma_bf16_tmem_a(d1, atl + 8 * ks, bh, id1, 1u);
+            if (kXlo) mma_bf16_tmem_a(d1, ath + 8 * ks, bl0 + (uint64_t)(16 * ks), id1, 1u);
           }
           mma_commit(&bars[B_D1FULL]);
           if (i > 0) ok = gemm2(i - 1);
