@@ -223,9 +223,13 @@ def run_ours(args, ws, rank, gpu):
     g, s, ess, which = fit_stats(last, ds)
     ess_per_s = ess / s
     samp_s = float(np.max(last.seconds[:, 1])) if last.seconds.size else s
-    # roofline of the batched gradient kernel (dominant): 4 N K C flops per launch
+    # roofline of the batched gradient kernel (dominant): 4 N K flops per chain
+    # that requests a gradient; a launch serves the fit's active chains (all C
+    # at first, fewer as chains finish: the launch shrinks with them), so the
+    # per-launch work is taken at the fit's mean active chains per step
     N, K = ds.N, ds.K
-    flops = 4.0 * N * K * C
+    active_mean = grads_total / max(steps, 1)
+    flops = 4.0 * N * K * active_mean
     mean_ms = float(np.mean(grad_ms))
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
@@ -234,7 +238,8 @@ def run_ours(args, ws, rank, gpu):
     ach = flops / (mean_ms * 1e-3) / 1e12
     kpad = 16 * ((K + 1 + 15) // 16)
     tensor = args.precision in ("bf16x3", "f16x3")
-    executed = 3 * 2 * 2.0 * N * C * kpad  # three 16-bit products, two contractions, K padded
+    # three 16-bit products, two contractions, K padded (active chains)
+    executed = 3 * 2 * 2.0 * N * active_mean * kpad
     traffic = TRAFFIC.get((args.workload, args.precision))
     roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
             "frac": ach / peak,
@@ -246,7 +251,8 @@ def run_ours(args, ws, rank, gpu):
             "executed_tflops": executed / (mean_ms * 1e-3) / 1e12,
             "executed_frac": executed / (mean_ms * 1e-3) / 1e12 / peak,
             "mean_launch_ms": mean_ms,
-            "flops_per_launch": flops}
+            "flops_per_launch": flops,
+            "active_chains_per_launch": active_mean}
     out = {"metric": "grad evals/s", "value": value, "unit": "grad evals/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": secs_total * 1e3 / args.steps, "higher_is_better": True,

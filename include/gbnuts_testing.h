@@ -36,6 +36,15 @@ int gbnuts_sample_run_scripted(gbnuts_model* m, const gbnuts_run_config* cfg,
  * the launch ran and the device stayed usable. */
 int gbnuts_wait_probe(long long limit_cycles, int* code, int* completed);
 
+/* gbnuts_log_prob_grad_batch (propto, with Jacobian) over the points whose
+ * active[i] is non-zero, the way a sampler step evaluates the chains that
+ * request a gradient: in the narrow tensor-core forms the kernel packs the
+ * active points into as few 128-point groups as they fill (its planned
+ * launch).  lp and grad of inactive points are unspecified. */
+int gbnuts_log_prob_grad_batch_active(gbnuts_model* m, const double* theta, int num_points,
+                                      const int* active, int precision, double* lp,
+                                      double* grad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -400,6 +400,39 @@ static int eval_points(gbnuts_model* m, int C, const double* theta, int propto, 
   return check_device_error(m->ws);
 }
 
+int gbnuts_log_prob_grad_batch_active(gbnuts_model* m, const double* theta, int num_points,
+                                      const int* active, int precision, double* lp,
+                                      double* grad) {
+  if (!m || num_points <= 0 || !theta || !active || !lp || !grad)
+    return fail(GBNUTS_USAGE, "bad arguments");
+  const int C = num_points, D = m->desc.D;
+  int rc = ensure_precision(m, precision);
+  if (rc) return rc;
+  rc = ensure_scratch(m, C);
+  if (rc) return rc;
+  rc = prepare_workspace(m->desc, m->h_group_off.data(), C, precision, m->ws);
+  if (rc) return rc;
+  int* d_active = nullptr;
+  GBN_CUDA_TRY(cudaMalloc(&d_active, (size_t)C * sizeof(int)));
+  struct Free {
+    int* p;
+    ~Free() { cudaFree(p); }
+  } guard{d_active};
+  GBN_CUDA_TRY(cudaMemcpyAsync(d_active, active, (size_t)C * sizeof(int), cudaMemcpyHostToDevice,
+                               m->stream));
+  GBN_CUDA_TRY(cudaMemcpyAsync(m->d_theta, theta, (size_t)C * D * sizeof(double),
+                               cudaMemcpyHostToDevice, m->stream));
+  rc = launch_log_prob_grad(m->desc, precision, m->d_theta, D, C, d_active, m->d_lp, m->d_grad,
+                            D, 1, 1, m->ws, m->stream, nullptr, nullptr);
+  if (rc) return rc;
+  GBN_CUDA_TRY(cudaMemcpyAsync(lp, m->d_lp, C * sizeof(double), cudaMemcpyDeviceToHost,
+                               m->stream));
+  GBN_CUDA_TRY(cudaMemcpyAsync(grad, m->d_grad, (size_t)C * D * sizeof(double),
+                               cudaMemcpyDeviceToHost, m->stream));
+  GBN_CUDA_TRY(cudaStreamSynchronize(m->stream));
+  return check_device_error(m->ws);
+}
+
 int gbnuts_log_prob(gbnuts_model* m, const double* theta, int propto, int jacobian,
                     double* lp) {
   if (!lp) return fail(GBNUTS_USAGE, "lp is NULL");
@@ -718,7 +751,8 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   if (prc) return prc;
   prc = prepare_workspace(m->desc, m->h_group_off.data(), C, rc->precision, m->ws);
   if (prc) return prc;
-  const PartialsView pv{m->ws.partial, m->ws.NP, m->ws.S, m->ws.gz};
+  const PartialsView pv{m->ws.partial, m->ws.NP, m->ws.S, m->ws.gz,
+                        tct_dynamic(m->desc, rc->precision, C) ? m->ws.dyn : nullptr};
 
   int* h_done = nullptr;
   GBN_CUDA_TRY(cudaMallocHost(&h_done, sizeof(int)));

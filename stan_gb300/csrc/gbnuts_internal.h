@@ -82,6 +82,9 @@ struct GradWorkspace {
   // theta of the current request as tensor-core words, written by the step
   // kernel during a sampler run (null otherwise)
   const uint32_t* tc_words = nullptr;
+  // the narrow tensor-core kernel's plan in a sampler run (see launch_tct):
+  // [0] splits, [1] slot stride, [2 + c] chain c's slot; null otherwise
+  int* dyn = nullptr;
   std::vector<long long> h_split_rows;
   size_t bytes = 0;
 };
@@ -153,6 +156,16 @@ int block_chains(int K, int C);
 int tc_prepare(const ModelDesc& m, bool f16, void** xt, float** yt, int* n_tiles, int* x_exp,
                cudaStream_t st);
 int tct_splits(const ModelDesc& m, int C);
+// Sampler runs of up to kTctPlanMaxChains chains in the narrow tensor-core
+// form compact their active chains: the kernel packs the chains that request
+// a gradient into as few 128-chain groups as they fill and spreads its CTAs
+// over those groups' row splits, so a fit whose chains have partly finished
+// takes a shorter launch.  The plan (split count, slot stride, slot of each
+// chain) is written to ws.dyn for the step kernel's finalize.
+constexpr int kTctPlanMaxChains = 16384;
+inline bool tct_dynamic(const ModelDesc& m, int precision, int C);
+// CTAs of a planned launch (at least one per 128-chain group).
+int tct_plan_grid(int C);
 int launch_tct(const ModelDesc& m, int precision, const double* Q, int ldq, int C,
                const int* active, GradWorkspace& ws, cudaStream_t st);
 // Minimum rows per split of the CUDA-core gradient (0: the built-in rule).
@@ -169,6 +182,9 @@ inline bool tensor_form_supported(const ModelDesc& m) {
   return (m.link == LINK_LOGIT || m.link == LINK_POISSON_LOG) && m.off_z < 0;
 }
 inline bool is_tensor_precision(int p) { return p == 2 || p == 3 || p == 4; }
+inline bool tct_dynamic(const ModelDesc& m, int precision, int C) {
+  return is_tensor_precision(precision) && tc_supported(m) && C <= kTctPlanMaxChains;
+}
 // Wide-design form (glm_wide.cu, K + intercept > 128): one thread-block
 // cluster of F CTAs per (row split, 128 chains), a 128-feature slab per CTA.
 // wide_slabs: F (2 or 4), 0 when the design is outside the form's range.

@@ -98,6 +98,10 @@ struct TctArgs {
   double* P;
   int NP, S;
   int* err;
+  // planned launch (a sampler run, active non-null): the plan is written
+  // here ([0] splits, [1] slot stride, [2 + c] slot of chain c); null: the
+  // grid is (S splits, chain groups) and chain c's partials are slot c
+  int* dyn;
 };
 
 namespace tct {
@@ -190,19 +194,97 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + SMEM_BAR + 8 * B_COUNT);
   volatile int* abort_s = reinterpret_cast<volatile int*>(sm + SMEM_BAR + 8 * B_COUNT + 8);
   __shared__ int act_s[NCH];
+  __shared__ int chain_s[NCH];  // chain of each TMEM lane (M row)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int s = blockIdx.x;
-  const int c0 = blockIdx.y * NCH;
   const int hb = a.has_base;
   const int Kx = a.K + hb;
 
-  if (tid < NCH) {
-    const int cg = c0 + tid;
-    act_s[tid] = (cg < a.C) && (a.active == nullptr || a.active[cg] != 0);
+  // This CTA's row split s of S_eff, and its chain group gs: lanes
+  // 0..127 hold the chains of slots 128 gs .. 128 gs + 127, whose partials
+  // are rows s * slot_stride + slot of P.
+  int s, S_eff, gs;
+  size_t slot_stride;
+  if (a.dyn) {
+    // Planned: the chains requesting a gradient, in chain order, fill slots
+    // 0..n_act-1; the grid's CTAs are spread over their ceil(n_act / 128)
+    // groups.  Every CTA derives the same plan from the active flags.
+    __shared__ uint32_t bits_s[kTctPlanMaxChains / 32];
+    __shared__ int pre_s[kTctPlanMaxChains / 32 + 1];
+    const int W = (a.C + 31) / 32;
+    for (int w = warp; w < W; w += THREADS / 32) {
+      const int cg = 32 * w + lane;
+      const unsigned on = __ballot_sync(0xffffffffu, cg < a.C && a.active[cg] != 0);
+      if (lane == 0) bits_s[w] = on;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      // exclusive prefix of the words' active counts
+      int run = 0;
+      for (int w0 = 0; w0 < W; w0 += 32) {
+        const int w = w0 + lane;
+        const int cnt = w < W ? __popc(bits_s[w]) : 0;
+        int incl = cnt;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, off);
+          if (lane >= off) incl += v;
+        }
+        if (w < W) pre_s[w] = run + incl - cnt;
+        run += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      if (lane == 0) pre_s[W] = run;
+    }
+    __syncthreads();
+    const int n_act = pre_s[W];
+    if (n_act == 0) return;
+    const int g_act = (n_act + NCH - 1) / NCH;
+    S_eff = min(max(1, (int)gridDim.x / g_act), a.n_tiles);
+    gs = (int)blockIdx.x / S_eff;
+    s = (int)blockIdx.x - gs * S_eff;
+    if (gs >= g_act) return;
+    slot_stride = (size_t)NCH * g_act;
+    if (tid < NCH) {
+      const int slot = NCH * gs + tid;
+      int chain = 0, on = 0;
+      if (slot < n_act) {
+        // the word holding active chain #slot, then its bit
+        int lo = 0, hi = W - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (pre_s[mid] <= slot)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        uint32_t bb = bits_s[lo];
+        for (int j = slot - pre_s[lo]; j > 0; --j) bb &= bb - 1;
+        chain = 32 * lo + __ffs(bb) - 1;
+        on = 1;
+        if (s == 0) a.dyn[2 + chain] = slot;
+      }
+      act_s[tid] = on;
+      chain_s[tid] = chain;
+    }
+    if (blockIdx.x == 0 && tid == 0) {
+      a.dyn[0] = S_eff;
+      a.dyn[1] = (int)slot_stride;
+    }
+    __syncthreads();
+  } else {
+    s = blockIdx.x;
+    S_eff = a.S;
+    gs = blockIdx.y;
+    slot_stride = (size_t)a.C;
+    if (tid < NCH) {
+      const int cg = NCH * gs + tid;
+      act_s[tid] = (cg < a.C) && (a.active == nullptr || a.active[cg] != 0);
+      chain_s[tid] = cg < a.C ? cg : 0;
+    }
+    const int any = __syncthreads_or(tid < NCH ? act_s[tid] : 0);
+    if (!any) return;
   }
-  const int any = __syncthreads_or(tid < NCH ? act_s[tid] : 0);
-  if (!any) return;
+  const size_t row0_slot = (size_t)NCH * gs;  // slot of lane 0
 
   if (tid == 0) {
     for (int b = 0; b < STAGES; ++b) {
@@ -224,8 +306,8 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
   fence_after_sync();
   const uint32_t tmem = *tmem_slot;
 
-  const int t_begin = (int)((long long)a.n_tiles * s / a.S);
-  const int t_end = (int)((long long)a.n_tiles * (s + 1) / a.S);
+  const int t_begin = (int)((long long)a.n_tiles * s / S_eff);
+  const int t_end = (int)((long long)a.n_tiles * (s + 1) / S_eff);
   const int n = t_end - t_begin;
   constexpr bool kXlo = XLO && SPLIT;
   const uint32_t x_bytes = kXlo ? 2u * PART_BYTES : (uint32_t)PART_BYTES;
@@ -321,8 +403,8 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
       float eta_scale = 1.f;
       {
         const bool act = act_s[c] != 0;
-        const double* th = a.Q + (size_t)(act ? c0 + c : 0) * a.ldq;
-        const uint32_t* tw = a.QW ? a.QW + (size_t)(act ? c0 + c : 0) * kThetaWords : nullptr;
+        const double* th = a.Q + (size_t)(act ? chain_s[c] : 0) * a.ldq;
+        const uint32_t* tw = a.QW ? a.QW + (size_t)(act ? chain_s[c] : 0) * kThetaWords : nullptr;
         int e_c = 0;
         if (F16 && act) {
           if (tw) {
@@ -428,7 +510,7 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
           for (int j = 0; j < FW; ++j) g[j] *= gs;
         }
         if (act_s[c]) {
-          double* dst = a.P + ((size_t)s * a.C + c0 + c) * a.NP;
+          double* dst = a.P + ((size_t)s * slot_stride + row0_slot + c) * a.NP;
 #pragma unroll
           for (int j = 0; j < FW; ++j) {
             const int k = FW * sub + j;
@@ -444,7 +526,7 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
   fence_before_sync();
   __syncthreads();
   if (tid < NCH && act_s[tid]) {
-    double* dst = a.P + ((size_t)s * a.C + c0 + tid) * a.NP;
+    double* dst = a.P + ((size_t)s * slot_stride + row0_slot + tid) * a.NP;
     double lp = 0.0;
     if (n > 0)
       for (int k = 0; k < EPI_SUB; ++k) lp += sLP[k * NCH + tid];
@@ -459,6 +541,10 @@ __global__ void __launch_bounds__(tct::THREADS, 1) glm_tct_kernel(TctArgs a) {
     fence_after_sync();
     tmem_dealloc(tmem, 512);
   }
+}
+
+int tct_plan_grid(int C) {
+  return std::max(device_sm_count(), (C + tct::NCH - 1) / tct::NCH);
 }
 
 int tct_splits(const ModelDesc& m, int C) {
@@ -635,13 +721,15 @@ int launch_tct(const ModelDesc& m, int precision, const double* Q, int ldq, int 
   a.NP = ws.NP;
   a.S = ws.S;
   a.err = ws.err;
+  const bool planned = active != nullptr && ws.dyn != nullptr && tct_dynamic(m, precision, C);
+  a.dyn = planned ? ws.dyn : nullptr;
   if (a.xt == nullptr || a.yt == nullptr) {
     set_last_error("tensor-core tiles of X are not prepared for this precision");
     return GBNUTS_SOFTWARE;
   }
   const bool xlo = m.x_dtype != GBNUTS_BF16;
   const bool split = precision == GBNUTS_PREC_BF16X3;
-  dim3 grid(ws.S, (C + NCH - 1) / NCH);
+  dim3 grid = planned ? dim3(tct_plan_grid(C)) : dim3(ws.S, (C + NCH - 1) / NCH);
   if (f16) {
     if (m.link != LINK_LOGIT) {
       set_last_error("the f16x3 form takes the logistic GLM");

@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(128)
                            const int* __restrict__ active, const double* __restrict__ P,
                            int NP, int S, const double* __restrict__ Gz,
                            double* __restrict__ lp_out, double* __restrict__ grad, int ldg,
-                           int propto, int jacobian) {
+                           int propto, int jacobian, const int* __restrict__ dyn) {
   __shared__ double sh_cs[4][kMaxColSums];
   const int c = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(128)
   const Team tm{lane, 32, 1, nullptr};
   const double lp = finalize_chain(m, Q + (size_t)c * ldq, c, C, P, NP, S, Gz,
                                    grad + (size_t)c * ldg, 1.0, propto, jacobian, tm,
-                                   sh_cs[threadIdx.x >> 5]);
+                                   sh_cs[threadIdx.x >> 5], dyn);
   if (lane == 0) lp_out[c] = lp;
 }
 
@@ -476,7 +476,11 @@ int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int pre
   }
   const int S = choose_splits(m, C, precision);
   const int NP = n_partials(m);
-  size_t need = (size_t)S * C * NP * sizeof(double) +
+  // partial rows: [S][C] in the static layout; a planned narrow tensor-core
+  // launch writes at most 128 rows per CTA ([splits][slots])
+  const bool dyn = tct_dynamic(m, precision, C);
+  const size_t prow = std::max((size_t)S * C, dyn ? (size_t)128 * tct_plan_grid(C) : (size_t)0);
+  size_t need = prow * NP * sizeof(double) + (dyn ? (size_t)(2 + C) * sizeof(int) : 0) +
                 (m.off_z >= 0 ? (size_t)C * m.J * sizeof(double) : 0) +
                 (size_t)(S + 1) * sizeof(long long) + 16;
   if (ws.C == C && ws.S == S && ws.NP == NP && ws.partial && ws.precision == precision)
@@ -499,7 +503,12 @@ int prepare_workspace(const ModelDesc& m, const int* h_group_off, int C, int pre
   GBN_CUDA_TRY(cudaMalloc(&base, need));
   ws.bytes = need;
   ws.partial = reinterpret_cast<double*>(base);
-  size_t off = (size_t)S * C * NP * sizeof(double);
+  size_t off = prow * NP * sizeof(double);
+  if (dyn) {
+    ws.dyn = reinterpret_cast<int*>(base + off);
+    off += (size_t)(2 + C) * sizeof(int);
+    off = (off + 7) & ~(size_t)7;
+  }
   if (m.off_z >= 0) {
     ws.gz = reinterpret_cast<double*>(base + off);
     off += (size_t)C * m.J * sizeof(double);
@@ -550,9 +559,11 @@ int launch_log_prob_grad(const ModelDesc& m, int precision, const double* Q, int
                          cudaStream_t stream, cudaEvent_t ev0, cudaEvent_t ev1) {
   int rc = launch_partials(m, precision, Q, ldq, C, active, ws, stream, ev0, ev1);
   if (rc) return rc;
+  // a planned narrow tensor-core launch (active flags given) left its plan
+  const int* dyn = (active && ws.dyn && tct_dynamic(m, precision, C)) ? ws.dyn : nullptr;
   loglik_finalize_kernel<<<(C + 3) / 4, 128, 0, stream>>>(m, Q, ldq, C, active, ws.partial,
                                                           ws.NP, ws.S, ws.gz, lp, grad, ldg,
-                                                          propto, jacobian);
+                                                          propto, jacobian, dyn);
   GBN_CUDA_TRY(cudaGetLastError());
   return GBNUTS_OK;
 }

@@ -85,14 +85,22 @@ __device__ __forceinline__ void split_column_sums(const double* __restrict__ Pc,
 }
 
 // th: the chain's parameters; grad_out[d] = sign * d lp / d theta_d.  cs: the
-// team's shared buffer of kMaxColSums doubles.
+// team's shared buffer of kMaxColSums doubles.  dyn: the plan of a planned
+// narrow tensor-core launch (splits, slot stride, slot of each chain), or
+// null for partials [S][C][NP].
 __device__ __forceinline__ double finalize_chain(const ModelDesc& m, const double* th, int c,
                                                  int C, const double* __restrict__ P, int NP,
                                                  int S, const double* __restrict__ Gz,
                                                  double* grad_out, double sign, int propto,
-                                                 int jacobian, const Team& tm, double* cs) {
-  const size_t pstride = (size_t)C * NP;
+                                                 int jacobian, const Team& tm, double* cs,
+                                                 const int* dyn = nullptr) {
+  size_t pstride = (size_t)C * NP;
   const double* Pc = P + (size_t)c * NP;
+  if (dyn) {
+    S = dyn[0];
+    pstride = (size_t)dyn[1] * NP;
+    Pc = P + (size_t)dyn[2 + c] * NP;
+  }
   const bool use_cs = NP <= kMaxColSums;
   if (use_cs) split_column_sums(Pc, pstride, S, NP, cs, tm);
   // sum over splits of partial column k (split order when lanes run over columns)

@@ -738,7 +738,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
   // partials into the working point's g slot (g = -grad lp); returns V.
   auto resume = [&](int q_slot, int g_slot) -> double {
     const double lp = finalize_chain(m, x.slot(q_slot), c, cfg.C, pv.P, pv.NP, pv.S, pv.Gz,
-                                     x.slot(g_slot), -1.0, 1, 1, tm, cs_s);
+                                     x.slot(g_slot), -1.0, 1, 1, tm, cs_s, pv.dyn);
     if (isnan(lp)) return lp;
     if (!isfinite(lp)) return inf;
     return -lp;

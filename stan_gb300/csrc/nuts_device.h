@@ -90,6 +90,8 @@ struct PartialsView {
   const double* P;
   int NP, S;
   const double* Gz;
+  // a planned narrow tensor-core launch's plan (GradWorkspace::dyn), or null
+  const int* dyn;
 };
 
 // Device pointers of one fit's sampler state and gradient stage.

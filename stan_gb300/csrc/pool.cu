@@ -312,7 +312,7 @@ static int rebuild_tables(gbnuts_pool* p) {
     pf.cfg = f->cfg;
     pf.m = f->model->desc;
     pf.f = FitPtrs{f->states, f->stacks, f->vecs, f->req,
-                   PartialsView{f->P, f->NP, f->S, f->Gz},
+                   PartialsView{f->P, f->NP, f->S, f->Gz, nullptr},
                    f->active, f->draws, f->diag, f->init_out, f->inits,
                    p->d_done + f->slot, p->d_abort + f->slot};
     fits.push_back(pf);

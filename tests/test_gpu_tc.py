@@ -71,6 +71,51 @@ def test_split_gradient_matches_fp64_oracle(kind, precision):
         assert np.linalg.norm(g[c] - go) <= 1e-4 * np.linalg.norm(go), c
 
 
+@pytest.mark.parametrize("precision", ["f16x3", "bf16x3"])
+def test_planned_launch_packs_active_chains(precision):
+    """The sampler-step form of the tensor-core gradient: only the points
+    flagged active are evaluated, packed into as few 128-point groups as they
+    fill, the row splits spread over those groups (one group: every CTA on
+    it).  Each active point matches the FP64 oracle within the form's bounds,
+    and the full batch (the unplanned launch, other splits) closely."""
+    from stan_gb300 import Model, _lib
+    ds = make_dataset("logistic_100k", small=True, seed=9)
+    m = Model.from_dataset(ds)
+    om = ds.oracle_model()
+    C = 600
+    rng = np.random.default_rng(5)
+    th = rng.normal(size=(C, m.D)) * 0.3
+    lp_all, g_all = m.log_prob_grad_batch(th, precision)
+    lib = _lib.load()
+    f = lib.gbnuts_log_prob_grad_batch_active
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, dp, ctypes.c_int, ip, ctypes.c_int, dp, dp]
+    patterns = {
+        "all": np.ones(C, dtype=np.int32),
+        "every third": (np.arange(C) % 3 == 0).astype(np.int32),
+        "random 30%": (rng.random(C) < 0.3).astype(np.int32),
+        "last only": (np.arange(C) == C - 1).astype(np.int32),
+        "one group's worth, scattered": np.isin(np.arange(C), rng.choice(C, 128, replace=False)
+                                                ).astype(np.int32),
+    }
+    for name, act in patterns.items():
+        lp = np.zeros(C)
+        g = np.zeros((C, m.D))
+        rc = f(m._h, th.ctypes.data_as(dp), C, act.ctypes.data_as(ip), _lib.PRECISIONS[precision],
+               lp.ctypes.data_as(dp), g.ctypes.data_as(dp))
+        assert rc == 0, _lib.last_error()
+        on = np.flatnonzero(act)
+        for c in on:
+            assert abs(lp[c] - lp_all[c]) <= 1e-6 * abs(lp_all[c]), (name, c)
+            assert np.linalg.norm(g[c] - g_all[c]) <= 2e-5 * np.linalg.norm(g_all[c]), (name, c)
+        for c in on[:: max(1, len(on) // 12)]:
+            lpo, go = om.log_prob_grad(th[c])
+            assert abs(lp[c] - lpo) <= 1e-5 * abs(lpo), (name, c)
+            assert np.linalg.norm(g[c] - go) <= 1e-4 * np.linalg.norm(go), (name, c)
+
+
 def test_bf16x3_full_size_logistic():
     """N = 100000, K = 100 at 1024 chains (the benchmark shape)."""
     from stan_gb300 import Model
