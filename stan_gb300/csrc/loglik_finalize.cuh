@@ -22,14 +22,17 @@ static constexpr int kMaxColSums = 4 + 512;
 static constexpr int kLanesOverSplits = 32;
 
 // Column sums over the S splits of one chain's partials (row stride pstride)
-// into cs[k], k < NP.  With many splits: lanes over splits and a fixed
-// butterfly per column.  Otherwise lanes over columns (or column pairs, as
-// 16-byte loads, when the rows are 16-byte aligned), adding the splits in
-// split order, their loads issued ten (eight) at a time.  The order of
-// additions depends on S and NP only.
+// into cs[k], k < NP.  Lanes over column pairs, as 16-byte loads, when the
+// rows are 16-byte aligned and that takes no more rounds of loads than lanes
+// over splits; with many splits otherwise: lanes over splits and a fixed
+// butterfly per column; else lanes over columns.  Over columns the splits
+// are added in split order, their loads issued ten (eight) at a time.  The
+// order of additions depends on S, NP and the team size only.
 __device__ __forceinline__ void split_column_sums(const double* __restrict__ Pc, size_t pstride,
                                                   int S, int NP, double* cs, const Team& tm) {
-  if (S < kLanesOverSplits && ((NP | (int)(pstride & 1)) & 1) == 0 &&
+  const int pair_rounds = ((NP / 2 + tm.n - 1) / tm.n) * ((S + 9) / 10);
+  const int split_rounds = S >= kLanesOverSplits ? (NP + tm.nw - 1) / tm.nw : 1 << 30;
+  if (pair_rounds <= split_rounds && ((NP | (int)(pstride & 1)) & 1) == 0 &&
       (reinterpret_cast<uintptr_t>(Pc) & 15) == 0) {
     const int npair = NP >> 1;
     const size_t ps2 = pstride >> 1;
