@@ -419,13 +419,15 @@ int launch_partials_pool(const PoolGradFit* d_fits, const PoolWorkItem* d_items,
              : launch_pool_cb<uint16_t, float>(d_fits, d_items, n_items, cb, smem, st);
 }
 
-// Minimum rows of a split: the built-in 256, or the value set through
-// gbnuts_set_launch_shape (for tuning).
+// Minimum rows of a split: the built-in 256 (32 for the FP64 form, whose
+// rows cost GB300's FP64 pipe ~20x an FP32 row: a small fit's gradient then
+// spreads over more SMs), or the value set through gbnuts_set_launch_shape
+// (for tuning).
 static std::atomic<long long> g_split_rows_min{0};
 void set_split_rows_min(long long rows) { g_split_rows_min.store(rows > 0 ? rows : 0); }
-static long long split_rows_min() {
+static long long split_rows_min(int precision) {
   const long long r = g_split_rows_min.load();
-  return r > 0 ? r : 256LL;
+  return r > 0 ? r : (precision == GBNUTS_PREC_FP64 ? 32LL : 256LL);
 }
 
 int choose_splits(const ModelDesc& m, int C, int precision) {
@@ -438,7 +440,7 @@ int choose_splits(const ModelDesc& m, int C, int precision) {
   const int chain_blocks = (C + CB - 1) / CB;
   // Splits: enough CTAs for ~2 waves over the SMs, a minimum of rows each.
   const int sms = device_sm_count();
-  long long max_s = std::max(1LL, m.N / split_rows_min());
+  long long max_s = std::max(1LL, m.N / split_rows_min(precision));
   int S = (int)std::min<long long>(max_s, std::max(1, (2 * sms + chain_blocks - 1) / chain_blocks));
   if (m.off_z >= 0) S = std::min(S, m.J);
   S = std::max(S, 1);
