@@ -157,11 +157,15 @@ enum { GBNUTS_DEBUG = 0, GBNUTS_INFO = 1, GBNUTS_WARN = 2, GBNUTS_ERROR = 3, GBN
  * write_blank; logger.{debug..fatal} is log; interrupt() returning nonzero
  * aborts (the interface throwing from interrupt, generate_transitions.hpp:52);
  * structured_writer's {stepsize, metric_type, inv_metric} record
- * (base_hmc.hpp:70-76) is write_metric.  Callbacks run after the device run,
- * chain by chain in chain order on the calling thread; or, when
- * chains_concurrent is nonzero, the writers of different chains may be called
- * from different threads at once (each chain's calls stay in order on one
- * thread, as in the reference's per-chain TBB tasks), and log must then be
+ * (base_hmc.hpp:70-76) is write_metric.  In the service functions the
+ * writers receive each chain's init values, names, rows and adaptation block
+ * while the device run goes on, from a host drain thread (once every chain
+ * has initialised), and the rest (remaining rows, timing, log messages) after
+ * it on the calling thread; interrupt is called on the calling thread between
+ * step chunks.  With chains_concurrent zero the writers are called from one
+ * thread at a time; when it is nonzero, the writers of different chains may be
+ * called from different threads at once (each chain's calls stay in order,
+ * as in the reference's per-chain TBB tasks), and log must then be
  * thread-safe. */
 typedef struct {
   void* ctx;

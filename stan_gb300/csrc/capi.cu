@@ -163,6 +163,18 @@ static thread_local struct {
   int len = 0;
 } g_draw_script;
 
+// Mapped host arrays of the service's host drain for the next
+// gbnuts_sample_run on this thread (device-side pointers), or null.
+struct DrainPtrs {
+  double* rows;
+  double* diag;
+  int* count;
+  double* init;
+  double* adapt;
+  int* flag;
+};
+static thread_local const DrainPtrs* g_drain = nullptr;
+
 // Read-only view of a model for the no-allocation entry point (noalloc.cu).
 int gbnuts_internal_model_view(const gbnuts_model* m, gbn::ModelDesc* desc,
                                const int** group_off) {
@@ -788,6 +800,14 @@ extern "C" int gbnuts_sample_run(gbnuts_model* m, const gbnuts_run_config* rc,
   h_fit.f = FitPtrs{d_states, d_stacks, d_vecs, d_req, pv, d_active, d_draws,
                     d_diag, d_init, d_inits, d_done, d_abort};
   h_fit.f.dense = d_dense;
+  if (g_drain) {
+    h_fit.f.h_rows = g_drain->rows;
+    h_fit.f.h_diag = d_diag ? g_drain->diag : nullptr;
+    h_fit.f.h_count = g_drain->count;
+    h_fit.f.h_init = g_drain->init;
+    h_fit.f.h_adapt = g_drain->adapt;
+    h_fit.f.h_flag = g_drain->flag;
+  }
   // the tensor-memory gradient kernel reads the request as packed words
   uint32_t* d_reqw = nullptr;
   struct WordsGuard {
@@ -1034,8 +1054,225 @@ void write_timing(const gbnuts_callbacks* cb, int c, int w, double warm, double 
   emit_blank(cb, c, w);
 }
 
+// What a chain's writers have received so far: the host drain writes during
+// the run, write_run completes the chain after it.
+struct ChainEmit {
+  bool init = false;   // init values
+  bool names = false;  // header names
+  int rows = 0;        // rows
+  bool adapt = false;  // adaptation block
+};
+
 int write_run(const gbnuts_model* m, const gbnuts_run_config& rc, const gbnuts_run_output& o,
-              const gbnuts_callbacks* cb);
+              const gbnuts_callbacks* cb, const std::vector<ChainEmit>* prior = nullptr);
+
+// The service's writer protocol pieces shared by the drain and write_run.
+struct WriterNames {
+  std::vector<std::string> sample, diagnostic;
+  explicit WriterNames(const ModelDesc& desc) {
+    std::vector<std::string> cnames, unames;
+    host_names(desc, true, cnames);
+    host_names(desc, false, unames);
+    const std::vector<std::string> sn = {"lp__", "accept_stat__", "stepsize__", "treedepth__",
+                                         "n_leapfrog__", "divergent__", "energy__"};
+    sample = sn;
+    sample.insert(sample.end(), cnames.begin(), cnames.end());
+    diagnostic = sn;
+    for (auto& s : unames) diagnostic.push_back(s);
+    for (auto& s : unames) diagnostic.push_back("p_" + s);
+    for (auto& s : unames) diagnostic.push_back("g_" + s);
+  }
+};
+
+// One row to the sample writer (and, with diag, the diagnostic writer: the
+// sampler columns, then q, p, g).
+void emit_row(const gbnuts_callbacks* cb, int c, const double* row, int n_cols,
+              const double* diag, int D, std::vector<double>& drow) {
+  emit_values(cb, c, GBNUTS_SAMPLE_WRITER, row, n_cols);
+  if (diag) {
+    drow.resize(7 + 3 * D);
+    memcpy(drow.data(), row, 7 * sizeof(double));
+    memcpy(drow.data() + 7, diag, 3 * D * sizeof(double));
+    emit_values(cb, c, GBNUTS_DIAGNOSTIC_WRITER, drow.data(), 7 + 3 * D);
+  }
+}
+
+// mcmc_writer::write_adapt_finish + base_hmc::write_sampler_state; invm
+// row-major (D values for diag_e, D x D for dense_e).
+void emit_adapt_block(const gbnuts_callbacks* cb, int c, const gbnuts_run_config& rc, int D,
+                      double eps, const double* invm) {
+  emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Adaptation terminated");
+  emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Step size = " + fmt(eps));
+  if (rc.metric == GBNUTS_METRIC_DENSE) {
+    // dense_e_point::write_metric (dense_e_point.hpp:35-48)
+    emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Elements of inverse mass matrix:");
+    if (D == 0) emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "");
+    for (int i = 0; i < D; ++i) {
+      std::ostringstream s;
+      for (int j = 0; j < D; ++j) s << (j ? ", " : "") << invm[(size_t)i * D + j];
+      emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, s.str());
+    }
+    if (rc.adapt && cb && cb->write_metric) cb->write_metric(cb->ctx, c, eps, "dense_e", invm, D * D);
+  } else {
+    emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Diagonal elements of inverse mass matrix:");
+    std::ostringstream s;
+    for (int d = 0; d < D; ++d) s << (d ? ", " : "") << invm[d];
+    emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, s.str());
+    if (rc.adapt && cb && cb->write_metric) cb->write_metric(cb->ctx, c, eps, "diag_e", invm, D);
+  }
+}
+
+// The service's host drain: the step kernel also writes every row, the init
+// values and the end-of-warmup adaptation record into mapped host memory
+// (DrainPtrs), each followed by a count or flag; host threads poll those and
+// pass what has arrived to the writer callbacks while the device run goes on
+// (chain c's calls in order, on thread c mod n).  Nothing is written until
+// every chain has initialised (a failed initialisation reports only errors,
+// as the reference's set-up does).  write_run completes each chain after the
+// run from where the drain stopped.
+class HostDrain {
+ public:
+  HostDrain(const gbnuts_model* m, const gbnuts_run_config& rc, const gbnuts_callbacks* cb,
+            int max_rows, bool diag)
+      : m_(m), rc_(rc), cb_(cb), C_(rc.num_chains), D_(m->desc.D), n_cols_(7 + m->desc.D),
+        max_rows_(max_rows), names_(m->desc), emit_(rc.num_chains) {
+    const int M = rc.metric == GBNUTS_METRIC_DENSE ? D_ * D_ : D_;
+    adapt_stride_ = 1 + M;
+    bytes_rows_ = (size_t)C_ * max_rows_ * n_cols_ * sizeof(double);
+    bytes_diag_ = diag ? (size_t)C_ * max_rows_ * 3 * D_ * sizeof(double) : 0;
+    const size_t bytes = bytes_rows_ + bytes_diag_ + (size_t)C_ * D_ * sizeof(double) +
+                         (size_t)C_ * adapt_stride_ * sizeof(double) + (size_t)3 * C_ * sizeof(int);
+    if (cudaHostAlloc(&base_, bytes, cudaHostAllocMapped) != cudaSuccess) {
+      cudaGetLastError();
+      base_ = nullptr;
+      return;
+    }
+    char* p = static_cast<char*>(base_);
+    rows_ = reinterpret_cast<double*>(p);
+    p += bytes_rows_;
+    diag_ = diag ? reinterpret_cast<double*>(p) : nullptr;
+    p += bytes_diag_;
+    init_ = reinterpret_cast<double*>(p);
+    p += (size_t)C_ * D_ * sizeof(double);
+    adapt_ = reinterpret_cast<double*>(p);
+    p += (size_t)C_ * adapt_stride_ * sizeof(double);
+    count_ = reinterpret_cast<int*>(p);
+    flag_ = count_ + C_;
+    memset(count_, 0, (size_t)3 * C_ * sizeof(int));
+    void* d = nullptr;
+    if (cudaHostGetDevicePointer(&d, base_, 0) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFreeHost(base_);
+      base_ = nullptr;
+      return;
+    }
+    const ptrdiff_t off = static_cast<char*>(d) - static_cast<char*>(base_);
+    auto dev = [&](void* h) { return static_cast<char*>(h) + off; };
+    ptrs_.rows = reinterpret_cast<double*>(dev(rows_));
+    ptrs_.diag = diag_ ? reinterpret_cast<double*>(dev(diag_)) : nullptr;
+    ptrs_.count = reinterpret_cast<int*>(dev(count_));
+    ptrs_.init = reinterpret_cast<double*>(dev(init_));
+    ptrs_.adapt = reinterpret_cast<double*>(dev(adapt_));
+    ptrs_.flag = reinterpret_cast<int*>(dev(flag_));
+  }
+  ~HostDrain() {
+    stop();
+    if (base_) cudaFreeHost(base_);
+  }
+  bool ok() const { return base_ != nullptr; }
+  const DrainPtrs* ptrs() const { return &ptrs_; }
+
+  void start() {
+    const int nt = (cb_ && cb_->chains_concurrent)
+                       ? std::min(C_, std::max(1, (int)std::thread::hardware_concurrency()))
+                       : 1;
+    for (int t = 0; t < nt; ++t)
+      threads_.emplace_back([this, t, nt] {
+        std::vector<double> drow;
+        while (!stop_.load(std::memory_order_acquire)) {
+          if (gate()) {
+            for (int c = t; c < C_; c += nt) {
+              try {
+                pump(c, drow);
+              } catch (...) {
+              }
+            }
+          }
+          std::this_thread::sleep_for(std::chrono::microseconds(500));
+        }
+      });
+  }
+  void stop() {
+    stop_.store(true, std::memory_order_release);
+    for (auto& t : threads_) t.join();
+    threads_.clear();
+  }
+  const std::vector<ChainEmit>& emitted() const { return emit_; }
+
+ private:
+  int load(const int* p) const { return *reinterpret_cast<const volatile int*>(p); }
+  // open once every chain has written its init values
+  bool gate() {
+    if (open_.load(std::memory_order_acquire)) return true;
+    for (int c = 0; c < C_; ++c)
+      if (!load(flag_ + 2 * c)) return false;
+    std::atomic_thread_fence(std::memory_order_acquire);
+    open_.store(true, std::memory_order_release);
+    return true;
+  }
+  void pump(int c, std::vector<double>& drow) {
+    ChainEmit& e = emit_[c];
+    if (!e.init) {
+      emit_values(cb_, c, GBNUTS_INIT_WRITER, init_ + (size_t)c * D_, D_);
+      e.init = true;
+    }
+    const int count = std::min(load(count_ + c), max_rows_);
+    std::atomic_thread_fence(std::memory_order_acquire);
+    if (count <= e.rows) return;
+    if (!e.names) {
+      emit_names(cb_, c, GBNUTS_SAMPLE_WRITER, names_.sample);
+      emit_names(cb_, c, GBNUTS_DIAGNOSTIC_WRITER, names_.diagnostic);
+      e.names = true;
+    }
+    const int thin = std::max(1, rc_.num_thin);
+    const int n_warm = rc_.save_warmup ? (rc_.num_warmup + thin - 1) / thin : 0;
+    while (e.rows < count) {
+      if (e.rows == n_warm && !e.adapt) {
+        if (!load(flag_ + 2 * c + 1)) return;
+        std::atomic_thread_fence(std::memory_order_acquire);
+        const double* rec = adapt_ + (size_t)c * adapt_stride_;
+        if (rc_.metric == GBNUTS_METRIC_DENSE) {
+          // the record is column-major; the block prints it row-major
+          std::vector<double> a((size_t)D_ * D_);
+          for (int i = 0; i < D_; ++i)
+            for (int j = 0; j < D_; ++j) a[(size_t)i * D_ + j] = rec[1 + (size_t)j * D_ + i];
+          emit_adapt_block(cb_, c, rc_, D_, rec[0], a.data());
+        } else {
+          emit_adapt_block(cb_, c, rc_, D_, rec[0], rec + 1);
+        }
+        e.adapt = true;
+      }
+      const size_t ri = (size_t)c * max_rows_ + e.rows;
+      emit_row(cb_, c, rows_ + ri * n_cols_, n_cols_, diag_ ? diag_ + ri * 3 * D_ : nullptr, D_,
+               drow);
+      ++e.rows;
+    }
+  }
+
+  const gbnuts_model* m_;
+  gbnuts_run_config rc_;
+  const gbnuts_callbacks* cb_;
+  int C_, D_, n_cols_, max_rows_, adapt_stride_ = 0;
+  WriterNames names_;
+  std::vector<ChainEmit> emit_;
+  void* base_ = nullptr;
+  size_t bytes_rows_ = 0, bytes_diag_ = 0;
+  double *rows_ = nullptr, *diag_ = nullptr, *init_ = nullptr, *adapt_ = nullptr;
+  int *count_ = nullptr, *flag_ = nullptr;
+  DrainPtrs ptrs_{};
+  std::vector<std::thread> threads_;
+  std::atomic<bool> stop_{false}, open_{false};
+};
 
 int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* cb) {
   const int C = rc.num_chains, D = m ? m->desc.D : 0;
@@ -1065,7 +1302,16 @@ int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* c
   o.init = init.data();
   o.n_grad = ngrad.data();
   o.seconds = secs.data();
+  // rows reach the writers while the run goes on (when mapped host memory
+  // can be had; otherwise all of them after it)
+  HostDrain drain(m, rc, cb, o.max_rows, diag);
+  if (drain.ok()) {
+    g_drain = drain.ptrs();
+    drain.start();
+  }
   int r = gbnuts_sample_run(m, &rc, &o, cb);
+  g_drain = nullptr;
+  drain.stop();
   if (r == GBNUTS_CONFIG) {
     emit_log(cb, GBNUTS_ERROR, last_error());
     return r;
@@ -1086,7 +1332,7 @@ int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* c
       return GBNUTS_CONFIG;
     }
   }
-  return write_run(m, rc, o, cb);
+  return write_run(m, rc, o, cb, drain.ok() ? &drain.emitted() : nullptr);
 }
 
 // Writes a finished run through the writer callbacks in the service protocol
@@ -1094,7 +1340,7 @@ int run_service(gbnuts_model* m, gbnuts_run_config rc, const gbnuts_callbacks* c
 // init values, the names, warmup rows, the adaptation block, sampling rows and
 // the timing block, with the reference's messages for failed chains.
 int write_run(const gbnuts_model* m, const gbnuts_run_config& rc, const gbnuts_run_output& o,
-              const gbnuts_callbacks* cb) {
+              const gbnuts_callbacks* cb, const std::vector<ChainEmit>* prior) {
   const int C = rc.num_chains, D = m->desc.D, n_cols = 7 + D;
   const bool diag = cb && cb->want_diagnostics && o.diagnostics;
   const int* status = o.status;
@@ -1104,70 +1350,35 @@ int write_run(const gbnuts_model* m, const gbnuts_run_config& rc, const gbnuts_r
   const double* invm = o.inv_metric;
   const double* init = o.init;
   const double* secs = o.seconds;
-  std::vector<std::string> cnames, unames;
-  host_names(m->desc, true, cnames);
-  host_names(m->desc, false, unames);
-  std::vector<std::string> sample_names = {"lp__", "accept_stat__", "stepsize__", "treedepth__",
-                                           "n_leapfrog__", "divergent__", "energy__"};
-  std::vector<std::string> snames = sample_names;
-  snames.insert(snames.end(), cnames.begin(), cnames.end());
-  std::vector<std::string> dnames = sample_names;
-  for (auto& s : unames) dnames.push_back(s);
-  for (auto& s : unames) dnames.push_back("p_" + s);
-  for (auto& s : unames) dnames.push_back("g_" + s);
-  // one chain's rows and messages, in the reference's order; chains touch
-  // only their own writers
+  const WriterNames names(m->desc);
+  // one chain's rows and messages, in the reference's order, from where the
+  // drain (if any) stopped; chains touch only their own writers
   auto emit_chain = [&](int c) -> int {
+    const ChainEmit e = prior ? (*prior)[c] : ChainEmit();
     std::vector<double> drow(7 + 3 * D);
-    emit_values(cb, c, GBNUTS_INIT_WRITER, init + (size_t)c * D, D);
+    if (!e.init) emit_values(cb, c, GBNUTS_INIT_WRITER, init + (size_t)c * D, D);
     if (status[c] == GBNUTS_CHAIN_STEPSIZE_INIT_FAILED) {
       // run_adaptive_sampler.hpp:61-68
       emit_log(cb, GBNUTS_ERROR, "Exception initializing step size.");
       emit_log(cb, GBNUTS_ERROR, "Posterior is improper. Please check your model.");
       return GBNUTS_OK;
     }
-    emit_names(cb, c, GBNUTS_SAMPLE_WRITER, snames);
-    emit_names(cb, c, GBNUTS_DIAGNOSTIC_WRITER, dnames);
+    if (!e.names) {
+      emit_names(cb, c, GBNUTS_SAMPLE_WRITER, names.sample);
+      emit_names(cb, c, GBNUTS_DIAGNOSTIC_WRITER, names.diagnostic);
+    }
     const double* base = o.draws + (size_t)c * o.max_rows * n_cols;
     auto write_rows = [&](int from, int to) {
-      for (int i = from; i < to; ++i) {
-        emit_values(cb, c, GBNUTS_SAMPLE_WRITER, base + (size_t)i * n_cols, n_cols);
-        if (diag) {
-          memcpy(drow.data(), base + (size_t)i * n_cols, 7 * sizeof(double));
-          memcpy(drow.data() + 7, o.diagnostics + ((size_t)c * o.max_rows + i) * 3 * D,
-                 3 * D * sizeof(double));
-          emit_values(cb, c, GBNUTS_DIAGNOSTIC_WRITER, drow.data(), 7 + 3 * D);
-        }
-      }
+      for (int i = from; i < to; ++i)
+        emit_row(cb, c, base + (size_t)i * n_cols, n_cols,
+                 diag ? o.diagnostics + ((size_t)c * o.max_rows + i) * 3 * D : nullptr, D, drow);
     };
-    write_rows(0, n_warm[c]);
+    write_rows(std::min(e.rows, n_warm[c]), n_warm[c]);
     const bool complete = status[c] == GBNUTS_CHAIN_OK;
-    if (complete || n_rows[c] > n_warm[c]) {
-      // mcmc_writer::write_adapt_finish + base_hmc::write_sampler_state
-      emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Adaptation terminated");
-      emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Step size = " + fmt(eps[c]));
-      if (rc.metric == GBNUTS_METRIC_DENSE) {
-        // dense_e_point::write_metric (dense_e_point.hpp:35-48)
-        const double* a = invm + (size_t)c * D * D;
-        emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Elements of inverse mass matrix:");
-        if (D == 0) emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "");
-        for (int i = 0; i < D; ++i) {
-          std::ostringstream s;
-          for (int j = 0; j < D; ++j) s << (j ? ", " : "") << a[(size_t)i * D + j];
-          emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, s.str());
-        }
-        if (rc.adapt && cb && cb->write_metric)
-          cb->write_metric(cb->ctx, c, eps[c], "dense_e", a, D * D);
-      } else {
-        emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, "Diagonal elements of inverse mass matrix:");
-        std::ostringstream s;
-        for (int d = 0; d < D; ++d) s << (d ? ", " : "") << invm[(size_t)c * D + d];
-        emit_msg(cb, c, GBNUTS_SAMPLE_WRITER, s.str());
-        if (rc.adapt && cb && cb->write_metric)
-          cb->write_metric(cb->ctx, c, eps[c], "diag_e", invm + (size_t)c * D, D);
-      }
-    }
-    write_rows(n_warm[c], n_rows[c]);
+    if (!e.adapt && (complete || n_rows[c] > n_warm[c]))
+      emit_adapt_block(cb, c, rc, D, eps[c],
+                       invm + (size_t)c * D * (rc.metric == GBNUTS_METRIC_DENSE ? D : 1));
+    write_rows(std::max(e.rows, n_warm[c]), n_rows[c]);
     if (status[c] == GBNUTS_CHAIN_OK) {
       write_timing(cb, c, GBNUTS_SAMPLE_WRITER, secs[2 * c], secs[2 * c + 1]);
       write_timing(cb, c, GBNUTS_DIAGNOSTIC_WRITER, secs[2 * c], secs[2 * c + 1]);

@@ -784,6 +784,14 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
           copy_vec(x, x.slot(SL_SMP_G), x.slot(SL_FWD_G));
           st.V_smp = V0;
           if (init_out) copy_vec(x, init_out + (size_t)c * D, x.slot(SL_SMP_Q));
+          if (f.h_init) {
+            // the init values for the host drain (util::initialize writes them
+            // to the init writer before the step size search)
+            copy_vec(x, f.h_init + (size_t)c * D, x.slot(SL_SMP_Q));
+            __threadfence_system();
+            tm.sync();
+            if (tid == 0) *reinterpret_cast<volatile int*>(f.h_flag + 2 * c) = 1;
+          }
           if (cfg.adapt) {
             st.ss_ctx = SS_CTX_START;
             st.phase = PH_SS_BEGIN;
@@ -888,6 +896,18 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
           st.warm_end_ngrad = st.n_grad;
         } else if (!cfg.adapt && st.iter == cfg.num_warmup && st.warm_end_ngrad < 0) {
           st.warm_end_ngrad = st.n_grad;
+        }
+        if (f.h_adapt && st.iter == cfg.num_warmup) {
+          // the adaptation record for the host drain: the step size and the
+          // inverse metric the sampling iterations use
+          const int M = x.dm ? D * D : D;
+          double* rec = f.h_adapt + (size_t)c * (1 + M);
+          const double* src = x.dm ? x.dm : x.slot(SL_INVM);
+          for (int i = tid; i < M; i += nth) rec[1 + i] = src[i];
+          if (tid == 0) rec[0] = st.nom_eps;
+          __threadfence_system();
+          tm.sync();
+          if (tid == 0) *reinterpret_cast<volatile int*>(f.h_flag + 2 * c + 1) = 1;
         }
         if (st.iter >= cfg.num_warmup + cfg.num_samples) {
           finish_chain(st, GBNUTS_CHAIN_OK, done_count, tid);
@@ -1099,6 +1119,14 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
           double* row = draws + ((size_t)c * cfg.max_rows + st.rows) * cfg.n_cols;
           double* dg = diag ? diag + ((size_t)c * cfg.max_rows + st.rows) * 3 * D : nullptr;
           write_row(x, st, row, dg);
+          if (f.h_rows) {
+            // the same row into the host drain's array, then the row count
+            const size_t ri = (size_t)c * cfg.max_rows + st.rows;
+            write_row(x, st, f.h_rows + ri * cfg.n_cols, f.h_diag ? f.h_diag + ri * 3 * D : nullptr);
+            __threadfence_system();
+            tm.sync();
+            if (tid == 0) *reinterpret_cast<volatile int*>(f.h_count + c) = st.rows + 1;
+          }
           st.rows += 1;
           if (m < cfg.num_warmup) st.warm_rows += 1;
         }

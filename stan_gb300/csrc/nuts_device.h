@@ -117,6 +117,19 @@ struct FitPtrs {
   // j * D + i): the inverse metric A, its Cholesky factor L (lower, A = L L^T)
   // and the Welford second-moment sums M2; null for diag_e
   double* dense;
+  // Service runs: what the writers need, also written to mapped host memory
+  // as it is produced, for the host drain that formats rows while the run
+  // goes on (null otherwise).  h_rows / h_diag: as draws / diag; h_count[c]:
+  // chain c's rows written; h_init [C][D]; h_adapt [C][1 + M]: the step size
+  // at the end of warmup, then the inverse metric (D values, or D x D
+  // column-major for dense_e); h_flag[2c] / h_flag[2c + 1]: init / adaptation
+  // record written.  Each flag or count is stored after a system-scope fence.
+  double* h_rows;
+  double* h_diag;
+  int* h_count;
+  double* h_init;
+  double* h_adapt;
+  int* h_flag;
 };
 
 void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* stacks,

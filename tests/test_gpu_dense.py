@@ -61,7 +61,7 @@ def test_dense_adaptive_run_replays_oracle():
     ordered differently) parts from the oracle's and adapts from a different
     trajectory, so: every chain's adapted step size within 10 %, and the chains
     that still track the oracle (step size to 1e-6; at least one) with the
-    adapted dense metric equal to 1e-6."""
+    adapted dense metric equal to 1e-6 (of its largest entry)."""
     from stan_gb300 import Model, sampler
     ds = make_dataset("logistic", small=True, seed=4)
     m = Model.from_dataset(ds)
@@ -77,7 +77,10 @@ def test_dense_adaptive_run_replays_oracle():
     assert np.all(rel < 0.1), rel
     track = rel < 1e-6
     assert track.any(), rel
-    assert np.allclose(r.inv_metric[track], o["inv_metric"][track], rtol=1e-6, atol=1e-12)
+    # entries near zero (cross covariances) carry the round-off at the
+    # matrix's scale
+    scale = np.abs(o["inv_metric"][track]).max()
+    assert np.allclose(r.inv_metric[track], o["inv_metric"][track], rtol=1e-6, atol=1e-6 * scale)
 
 
 def test_dense_posterior_matches_diag():

@@ -173,3 +173,43 @@ def test_interrupt_callback_stops_the_run():
     for w in sample:
         rows = [ln for ln in w.stream.getvalue().split("\n") if ln and not ln.startswith(("#", "lp__"))]
         assert len(rows) < 2000
+
+
+def test_rows_reach_the_writers_during_the_run():
+    """The host drain: rows go to the writer callbacks while the device run
+    is still going (the interrupt callback, polled between step chunks on the
+    calling thread, sees rows arrive), and the output equals the post-run
+    protocol's (every row once, in order, the adaptation block between the
+    warmup and sampling rows)."""
+    from stan_gb300 import Model, _lib, sampler, services
+    from stan_gb300.callbacks import StreamWriter
+    ds = make_dataset("logistic_100k", small=True, seed=7)
+    m = Model.from_dataset(ds)
+    C = 2
+    sample = [StreamWriter(io.StringIO()) for _ in range(C)]
+
+    def n_rows():
+        return sum(w.stream.getvalue().count("\n") for w in sample)
+
+    seen = []
+
+    class Watch:
+        def __call__(self):
+            seen.append(n_rows())
+            return False
+
+    kw = dict(KW, num_warmup=400, num_samples=400, save_warmup=1)
+    rc = services.hmc_nuts_diag_e_adapt(m, C, sample_writer=sample, interrupt=Watch(), **kw)
+    assert rc == _lib.OK
+    assert len(seen) > 3
+    assert any(0 < n < n_rows() for n in seen[:-1]), seen[:20]
+    ref = sampler.run(m, num_chains=C, **{k: v for k, v in kw.items()
+                                          if k not in ("init", "init_inv_metric", "refresh")})
+    for c in range(C):
+        lines = sample[c].stream.getvalue().split("\n")
+        rows = [ln for ln in lines if ln and not ln.startswith(("#", "lp__"))]
+        assert len(rows) == 800
+        i_adapt = next(i for i, ln in enumerate(lines) if ln == "# Adaptation terminated")
+        assert sum(1 for ln in lines[:i_adapt] if ln and not ln.startswith(("#", "lp__"))) == 400
+        got = np.array([[float(v) for v in ln.split(",")] for ln in rows])
+        assert np.allclose(got, ref.draws[c, :800], rtol=1e-5, atol=1e-6)
