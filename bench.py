@@ -412,6 +412,44 @@ def csv_leg(model, res, chains=256):
             shutil.rmtree(d, ignore_errors=True)
         report[label] = {"seconds": dt, "bytes": nbytes, "MB_per_s": nbytes / dt / 1e6,
                          "rows_per_s": rows / dt}
+    # The service writing the same kind of files for a fresh `chains`-chain
+    # fit: its rows are formatted while the device run goes on (the host
+    # drain), so the call takes about the fit's own time; the array run of
+    # the same fit, and writing its rows after it, for comparison.
+    from stan_gb300 import sampler, services
+    n_c = int(sub.num_chains)
+    kw = dict(random_seed=31, init_chain_id=1, init_radius=2.0, num_warmup=int(sub.num_warmup),
+              num_samples=int(sub.num_samples), num_thin=1, save_warmup=0, stepsize=1.0,
+              stepsize_jitter=0.0, max_depth=10, delta=0.8, gamma=0.05, kappa=0.75, t0=10.0,
+              init_buffer=75, term_buffer=50, window=25)
+    prec = {v: k for k, v in _lib.PRECISIONS.items()}[int(sub.precision)]
+    d = tempfile.mkdtemp(prefix="gbnuts_csv_")
+    try:
+        t0 = time.perf_counter()
+        rc = services.hmc_nuts_diag_e_adapt(model, n_c, None, None, refresh=0, precision=prec,
+                                            csv=CsvFiles(os.path.join(d, "svc")), **kw)
+        t_svc = time.perf_counter() - t0
+        _lib.check(rc, "gbnuts_hmc_nuts_diag_e_adapt")
+        svc_bytes = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d))
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    t0 = time.perf_counter()
+    r = sampler.run(model, num_chains=n_c, precision=prec, **kw)
+    t_arr = time.perf_counter() - t0
+    d = tempfile.mkdtemp(prefix="gbnuts_csv_")
+    try:
+        t0 = time.perf_counter()
+        sampler.write_csv(model, r, CsvFiles(os.path.join(d, "arr")))
+        t_write = time.perf_counter() - t0
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    report["service_drained"] = {
+        "chains": n_c, "bytes": svc_bytes, "service_call_s": t_svc,
+        "array_run_call_s": t_arr, "array_run_device_s": r.total_ms / 1e3,
+        "write_after_run_s": t_write,
+        "note": "service_call_s includes the run, formatting its rows while it goes on, and "
+                "the rest after it; array_run_call_s + write_after_run_s is the same work "
+                "done one after the other"}
     return report
 
 
