@@ -592,13 +592,17 @@ static __device__ bool merge_into_level(const Ctx& x, ChainState& st, const Stk&
     CR = x.slot(base_c + 5);
   }
   const double init_lsw = sk.lsw[l];
-  const double lsw_sub = log_sum_exp_d(init_lsw, cur_lsw);
+  // log-sum-exp and the acceptance probability, on one warp of the team
+  const double2 la = x.tm.one2([&]() {
+    const double s = log_sum_exp_d(init_lsw, cur_lsw);
+    return make_double2(s, cur_lsw > s ? 1.0 : exp(cur_lsw - s));
+  });
+  const double lsw_sub = la.x;
   bool sel_final;
   if (cur_lsw > lsw_sub) {
     sel_final = true;
   } else {
-    double accept_prob = exp(cur_lsw - lsw_sub);
-    sel_final = draw_uniform(cfg, st, x.c) < accept_prob;
+    sel_final = draw_uniform(cfg, st, x.c) < la.y;
   }
   const double* ps = nullptr;
   if (x.dm) {
@@ -646,14 +650,19 @@ static __device__ bool merge_top(const Ctx& x, ChainState& st, const Stk& sk, in
     CR = x.slot(base_c + 5);
   }
   st.depth += 1;
+  // the acceptance probability and the new log-sum-exp, on one warp
+  const double lsw_old = st.lsw;
+  const double2 al = x.tm.one2([&]() {
+    return make_double2(cur_lsw > lsw_old ? 1.0 : exp(cur_lsw - lsw_old),
+                        log_sum_exp_d(lsw_old, cur_lsw));
+  });
   bool sel;
   if (cur_lsw > st.lsw) {
     sel = true;
   } else {
-    double accept_prob = exp(cur_lsw - st.lsw);
-    sel = draw_uniform(cfg, st, x.c) < accept_prob;
+    sel = draw_uniform(cfg, st, x.c) < al.x;
   }
-  st.lsw = log_sum_exp_d(st.lsw, cur_lsw);
+  st.lsw = al.y;
   double* RHO = x.slot(SL_RHO);
   double* PFF = x.slot(SL_PFF);
   double* PFB = x.slot(SL_PFB);
@@ -1033,7 +1042,7 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
         if (w > 0)
           st.sum_metro += 1;
         else
-          st.sum_metro += exp(w);
+          st.sum_metro += tm.one([&]() { return exp(w); });
         if (st.divergent) {
           st.phase = PH_TRANS_END;
           break;

@@ -70,6 +70,37 @@ struct Team {
     sync();
   }
 
+  // f() on the team's first warp only, its value broadcast to every thread:
+  // scalar FP64 work (exp, log1p) that each warp would otherwise repeat on
+  // the SM's shared FP64 pipe.  Called by the whole team; slots 6 and 7 of
+  // the first warp's scratch are free of the sums above.
+  template <class F>
+  __device__ __forceinline__ double one(F f) const {
+    if (nw == 1) return f();
+    double v = 0.0;
+    if (t < 32) v = f();
+    if (t == 0) red[7] = v;
+    sync();
+    v = red[7];
+    sync();
+    return v;
+  }
+  // the same for a pair of values
+  template <class F>
+  __device__ __forceinline__ double2 one2(F f) const {
+    if (nw == 1) return f();
+    double2 v = make_double2(0.0, 0.0);
+    if (t < 32) v = f();
+    if (t == 0) {
+      red[6] = v.x;
+      red[7] = v.y;
+    }
+    sync();
+    v = make_double2(red[6], red[7]);
+    sync();
+    return v;
+  }
+
   __device__ __forceinline__ bool any(bool b) const {
     if (nw == 1) return __any_sync(0xffffffffu, b) != 0;
     unsigned r;
