@@ -512,7 +512,42 @@ def serving_leg(n_fits=None, rate=None, forms=None):
         summ["max_rhat_median_over_fits"] = float(np.median(list(rhat.values())))
         summ["max_rhat_max_over_fits"] = float(np.max(list(rhat.values())))
         out["mixed" if form == "fp32" else "fp64"] = summ
+    if "fp32" in forms:
+        out["precision_errors"] = serving_precision(dss, kw)
     return out
+
+
+def serving_precision(dss, kw, n=6):
+    """The mixed serving form's errors against the FP64 form on a spread of
+    the stream's fits (smallest to largest N): each fit runs alone in the
+    fp32 form with the stream's schedule, then at its chains' final draws
+    (and 64 points around them) log p and the gradient of both forms are
+    compared; the largest over the fits."""
+    from stan_gb300 import Model, sampler
+    order = np.argsort([d.N for d in dss])
+    pick = [int(order[int(round(i * (len(dss) - 1) / (n - 1)))]) for i in range(n)]
+    lp_max, g_max, dh = 0.0, 0.0, []
+    for i in pick:
+        m = Model.from_dataset(dss[i])
+        r = sampler.run(m, precision="fp32", **{k: v for k, v in kw.items() if k != "report_summary"})
+        C = r.draws.shape[0]
+        last = np.stack([r.draws[c, max(int(r.n_rows[c]) - 1, 0), 7:] for c in range(C)])
+        th0 = np.stack([m.unconstrain_array(last[c]) for c in range(C)])
+        th = th0[np.random.default_rng(i).integers(0, C, 64)] + \
+            np.random.default_rng(i + 1).normal(size=(64, m.D)) * 0.01
+        th = np.concatenate([th0, th])
+        lp32, g32 = m.log_prob_grad_batch(th, "fp32")
+        lp64, g64 = m.log_prob_grad_batch(th, "fp64")
+        lp_max = max(lp_max, float(np.max(np.abs(lp32 - lp64) / np.abs(lp64))))
+        g_max = max(g_max, float(np.max(np.linalg.norm(g32 - g64, axis=1) /
+                                        np.linalg.norm(g64, axis=1))))
+        dh.extend(np.abs(lp32[:C] - lp64[:C]).tolist())
+        m.close()
+    return {"vs": "fp64 GPU form", "fits": [int(dss[i].N) for i in pick],
+            "n_theta_per_fit": 64 + int(kw["num_chains"]), "lp_max_rel": lp_max,
+            "grad_max_rel": g_max,
+            "energy_abs_diff": {"n": len(dh), "median": float(np.median(dh)),
+                                "max": float(np.max(dh))}}
 
 
 def _moment_z(d_a, d_b):
