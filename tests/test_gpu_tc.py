@@ -219,8 +219,8 @@ def _errors(m, om, th, precision):
 @pytest.mark.parametrize("case", ["poisson_k512_bf16x", "logistic_k200_f32x",
                                   "logistic_k300_bf16x"])
 def test_wide_design_bf16_forms_match_fp64_oracle(case):
-    """K + intercept > 127: the thread-block-cluster kernel (a 128-feature slab
-    per CTA; X stored in fp32 runs as [hi | lo] features).  Split (bf16x3): lp
+    """K + intercept > 127: the wide-design kernel (32 chains per CTA, every
+    feature; X stored in fp32 runs as [hi | lo] features).  Split (bf16x3): lp
     within 1e-5, gradient within 1e-4 of the FP64 oracle; plain bf16: within
     2e-2."""
     from stan_gb300 import Model, workloads
@@ -232,7 +232,7 @@ def test_wide_design_bf16_forms_match_fp64_oracle(case):
         ds = workloads.logistic(2000, 300, seed=5, x_dtype="bf16")
     m = Model.from_dataset(ds)
     om = ds.oracle_model()
-    C = 130  # two chain blocks of 128, the second mostly empty
+    C = 130  # five blocks of 32 chains, the last mostly empty
     th = np.random.default_rng(6).normal(size=(C, m.D)) * (0.5 / np.sqrt(ds.K))
     e_lp, e_g = _errors(m, om, th, "bf16x3")
     assert e_lp <= 1e-5 and e_g <= 1e-4, (e_lp, e_g)
