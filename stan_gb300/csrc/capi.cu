@@ -88,7 +88,7 @@ static int ensure_precision(gbnuts_model* m, int precision) {
     return GBNUTS_OK;
   }
   if (!tc_supported(m->desc) && tensor_form_supported(m->desc)) {
-    // wide design: X as slab tiles for the cluster kernel
+    // wide design: X as slab tiles for the wide-design kernel
     if (m->d_wide_xt) return GBNUTS_OK;
     int tiles = 0;
     int rc = wide_prepare(m->desc, &m->d_wide_xt, &m->d_tc_yt, &tiles, m->stream);

@@ -185,9 +185,9 @@ inline bool is_tensor_precision(int p) { return p == 2 || p == 3 || p == 4; }
 inline bool tct_dynamic(const ModelDesc& m, int precision, int C) {
   return is_tensor_precision(precision) && tc_supported(m) && C <= kTctPlanMaxChains;
 }
-// Wide-design form (glm_wide.cu, K + intercept > 128): one thread-block
-// cluster of F CTAs per (row split, 128 chains), a 128-feature slab per CTA.
-// wide_slabs: F (2 or 4), 0 when the design is outside the form's range.
+// Wide-design form (glm_wide.cu, K + intercept > 128): one CTA per (row
+// split, 32 chains) with every feature, X in F 128-feature slabs per tile.
+// wide_slabs: F (4), 0 when the design is outside the form's range.
 // wide_splits: row splits S (the partials then hold S split rows, or 2 S
 // when X is not stored in bf16: hi and lo columns of the gradient).
 int wide_slabs(const ModelDesc& m);

@@ -432,7 +432,7 @@ static long long split_rows_min(int precision) {
 
 int choose_splits(const ModelDesc& m, int C, int precision) {
   if (is_tensor_precision(precision)) {
-    if (!tc_supported(m))  // wide-design cluster form
+    if (!tc_supported(m))  // wide-design form
       return wide_splits(m, C) * (m.x_dtype == GBNUTS_BF16 ? 1 : 2);
     return tct_splits(m, C);
   }
