@@ -401,10 +401,10 @@ int gbnuts_summary(const double* draws, int num_chains, int max_rows, int n_cols
 /* Launch-shape overrides, for tuning (no counterpart in the reference).
  * Process-wide; 0 restores the built-in rule.  split_rows_min: minimum rows
  * per row split of the CUDA-core gradient (fp64 / fp32 forms); team_warps:
- * warps per chain of the step kernel (1, 2 or 4).  A fit's splits fix the
+ * warps per chain of the step kernel (1, 2, 4 or 8).  A fit's splits fix the
  * order of its gradient sums, so a setting changes draws at round-off level
  * (runs stay deterministic for a fixed setting); change it between runs, not
- * while one is going.  USAGE for a team_warps other than 0, 1, 2, 4. */
+ * while one is going.  USAGE for a team_warps other than 0, 1, 2, 4, 8. */
 int gbnuts_set_launch_shape(long long split_rows_min, int team_warps);
 
 /* Device and build information: writes a short text description. */

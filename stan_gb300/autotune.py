@@ -7,8 +7,8 @@ the library's gbnuts_set_launch_shape(split_rows_min, team_warps):
                   (fp64 / fp32 forms; splits are also bounded by about two
                   waves of CTAs over the device's SMs and, for the
                   hierarchical families, by the group count)
-  team_warps      warps per chain of the step kernel (1, 2 or 4; by default
-                  1 up to D = 64, 2 up to 1024, 4 above)
+  team_warps      warps per chain of the step kernel (1, 2, 4 or 8; by
+                  default 1 up to D = 64, 2 up to 1024, 8 above)
 
 The setting is process-wide, so each candidate runs in its own process: a
 short adaptive fit of the workload, timed with CUDA events (device ms per
@@ -31,7 +31,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _ROOT = os.path.dirname(_HERE)
 
 SPLIT_ROWS = (64, 128, 256, 512, 1024)
-TEAM_WARPS = (1, 2, 4)
+TEAM_WARPS = (1, 2, 4, 8)
 
 
 def _candidate(args):

@@ -202,8 +202,8 @@ int gbnuts_sample_run_scripted(gbnuts_model* m, const gbnuts_run_config* cfg,
 
 int gbnuts_set_launch_shape(long long split_rows_min, int team_warps) {
   if (split_rows_min < 0 || !(team_warps == 0 || team_warps == 1 || team_warps == 2 ||
-                              team_warps == 4))
-    return fail(GBNUTS_USAGE, "split_rows_min >= 0 and team_warps in {0, 1, 2, 4}");
+                              team_warps == 4 || team_warps == 8))
+    return fail(GBNUTS_USAGE, "split_rows_min >= 0 and team_warps in {0, 1, 2, 4, 8}");
   set_split_rows_min(split_rows_min);
   set_team_warps(team_warps);
   return GBNUTS_OK;

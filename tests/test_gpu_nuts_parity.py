@@ -92,11 +92,12 @@ def test_draw_stream_matches_host():
         assert np.array_equal(r.init[c], (2.0 * u - 1.0) * 1.5)
 
 
-@pytest.mark.parametrize("J", [300, 1100])
-def test_multi_warp_chains_replay(J):
-    """Large dimensions run one chain per CTA of 2 (D <= 1024) or 4 warps;
-    their transitions replay the oracle like the warp-per-chain form."""
-    from stan_gb300 import Model, sampler, workloads
+@pytest.mark.parametrize("J,team", [(300, 0), (1100, 0), (1100, 4)])
+def test_multi_warp_chains_replay(J, team):
+    """Large dimensions run one chain per CTA of 2 (D <= 1024) or 8 warps
+    (team 0: the built-in rule; team 4 forces four warps); their transitions
+    replay the oracle like the warp-per-chain form."""
+    from stan_gb300 import Model, _lib, sampler, workloads
     ds = workloads.hier_normal(J=J, K=6, mean_size=4, seed=11)
     m = Model.from_dataset(ds)
     om = ds.oracle_model()
@@ -104,7 +105,12 @@ def test_multi_warp_chains_replay(J):
     inits = np.random.default_rng(2).normal(size=(C, m.D)) * 0.1
     kw = dict(num_chains=C, adapt=False, num_warmup=0, num_samples=4, stepsize=0.05,
               inits=inits, max_depth=6)
-    r = sampler.run(m, random_seed=9, **kw)
+    lib = _lib.load()
+    _lib.check(lib.gbnuts_set_launch_shape(0, team), "gbnuts_set_launch_shape")
+    try:
+        r = sampler.run(m, random_seed=9, **kw)
+    finally:
+        _lib.check(lib.gbnuts_set_launch_shape(0, 0), "gbnuts_set_launch_shape")
     o = om.sample(seed=9, **kw)
     assert np.all(r.status == 0) and np.all(o["return_code"] == 0)
     _compare(r, o, 4)
