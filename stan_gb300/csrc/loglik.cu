@@ -34,6 +34,21 @@ namespace gbn {
 
 static constexpr int kThreads = 256;
 static constexpr int kMaxPairs = 32;  // (chain, feature) adjoint pairs per thread
+// Designs of up to small_k_max<CT>() features take the per-thread row-run
+// form (small_k_rows): 16 in the fp32 form; none in the FP64 form, whose
+// kernel at 128 registers would spill its FP64 registers; its tiles hold up
+// to kSmallRunRows rows per thread run and about kSmallTileBytes of shared
+// memory.
+template <typename CT>
+__host__ __device__ constexpr int small_k_max() {
+  return sizeof(CT) == 8 ? 0 : 16;
+}
+template <typename CT>
+__host__ __device__ inline bool use_small_k(int K) {
+  return small_k_max<CT>() > 0 && K >= 1 && K <= small_k_max<CT>();
+}
+static constexpr int kSmallRunRows = 64;
+static constexpr size_t kSmallTileBytes = 64 * 1024;
 
 int chains_per_block(int K) {
   if (K <= 512) return 16;
@@ -47,14 +62,18 @@ int block_chains(int K, int C) {
   return std::min(chains_per_block(K), by_c);
 }
 
-template <typename XT>
-__device__ __forceinline__ double x_to_double(XT v);
+// X element in the compute type, converted once (fp32 X into the fp32 form
+// is a plain copy: no pass through double on GB300's FP64 pipe).
+template <typename CT, typename XT>
+__device__ __forceinline__ CT x_to(XT v) {
+  return (CT)v;
+}
 template <>
-__device__ __forceinline__ double x_to_double<double>(double v) { return v; }
+__device__ __forceinline__ float x_to<float, uint16_t>(uint16_t v) {
+  return __uint_as_float(((unsigned)v) << 16);
+}
 template <>
-__device__ __forceinline__ double x_to_double<float>(float v) { return (double)v; }
-template <>
-__device__ __forceinline__ double x_to_double<uint16_t>(uint16_t v) {
+__device__ __forceinline__ double x_to<double, uint16_t>(uint16_t v) {
   return (double)__uint_as_float(((unsigned)v) << 16);
 }
 
@@ -81,12 +100,225 @@ __device__ __forceinline__ void apply_link(int link, CT eta, CT y, CT inv_s2, CT
   }
 }
 
-// Shared memory of the partial kernel, in elements of the compute type.
+// Shared memory of the partial kernel: theta [CB][K + 1], then the tile's
+// rows (small-K form: [RB][KS], KS = K rounded up to 16-byte loads; otherwise
+// [RB][K + 1] and the residuals [RB][CB]), y, group.
+template <typename CT>
+__host__ __device__ inline int small_row_stride(int K) {
+  constexpr int VW = 16 / sizeof(CT);
+  return (K + VW - 1) / VW * VW;
+}
 template <typename CT>
 __host__ __device__ inline size_t partial_smem_bytes(int CB, int K, int RB) {
   const int KP = K + 1;
+  if (use_small_k<CT>(K))
+    return sizeof(CT) * ((size_t)CB * KP + (size_t)RB * small_row_stride<CT>(K) + RB) +
+           sizeof(int) * (size_t)RB;
   return sizeof(CT) * ((size_t)CB * KP + (size_t)RB * KP + (size_t)RB * CB + RB) +
          sizeof(int) * (size_t)RB;
+}
+
+// Designs of up to small_k_max<CT>() features (the hierarchical models'
+// group-level predictors): each thread owns one chain and a contiguous run of
+// RR = RB / RPT rows of every tile.  Theta, the K adjoint sums and the z of
+// the current group stay in registers (z is re-read and converted only when
+// the group changes); a row's features are 16-byte loads from shared memory,
+// and eta, the link and the adjoint update X^T r run in one pass over the row.
+// Group sums: a run's segments are summed in row order; a segment inside a run
+// is complete and written at once, and the first and last segments of the
+// runs are joined by one thread per chain in run order, carried across tiles.
+// Every sum's order depends on the split's rows only (deterministic).
+// Shared memory: th_s [CB][K + 1], then the tile's rows [RB][KS] (KS = K
+// rounded up to whole 16-byte loads), y, group (partial_smem_bytes).
+template <typename XT, typename CT, int CB>
+__device__ __forceinline__ void small_k_rows(
+    const ModelDesc& m, const double* __restrict__ Q, int ldq, int C, const CT* th_s,
+    const CT* base_s, const CT* tau_s, const CT* invs2_s, const int* act_s,
+    double (*red_s)[4], int RB, long long row_begin, long long row_end, double* __restrict__ P,
+    int NP, double* __restrict__ Gz, int s, int c0, double& lp_d, double& base_d,
+    double& tau_d, double& sq_d) {
+  constexpr int VW = 16 / sizeof(CT);   // elements per 16-byte load
+  constexpr int RPT = kThreads / CB;    // runs (threads) per chain
+  const int K = m.K, KP = K + 1;
+  const int KS = (K + VW - 1) / VW * VW;
+  const int RR = RB / RPT;
+  const int dr = kThreads / K, dk = kThreads - (kThreads / K) * K;
+  const int tid = threadIdx.x, my_c = tid % CB, my_rl = tid / CB;
+  CT* x_s = const_cast<CT*>(th_s) + (size_t)CB * KP;  // [RB][KS]
+  CT* y_s = x_s + (size_t)RB * KS;
+  int* g_s = reinterpret_cast<int*>(y_s + RB);
+  const XT* __restrict__ X = static_cast<const XT*>(m.X);
+  const bool has_z = m.off_z >= 0;
+  const bool cact = act_s[my_c] != 0;
+  struct RunEnds {  // one run's group segments at its two ends (red_s: 32 bytes a thread)
+    int fkey, lkey;
+    CT fsum, lsum;
+  };
+  static_assert(sizeof(RunEnds) <= 4 * sizeof(double), "run ends fit a red_s row");
+  const int cg = c0 + my_c;
+  const double* thq = Q + (size_t)(cact ? cg : 0) * ldq;
+
+  constexpr int SK = small_k_max<CT>() > 0 ? small_k_max<CT>() : 1;
+  CT th[SK], acc[SK];
+#pragma unroll
+  for (int k = 0; k < SK; ++k) {
+    th[k] = k < K ? th_s[my_c * KP + k] : CT(0);
+    acc[k] = CT(0);
+  }
+  // feature columns K .. KS-1 stay zero
+  for (int idx = tid; idx < RB * (KS - K); idx += kThreads) {
+    const int r = idx / (KS - K);
+    x_s[r * KS + K + (idx - r * (KS - K))] = CT(0);
+  }
+  const CT base = base_s[my_c], tau = tau_s[my_c], invs2 = invs2_s[my_c];
+  int zkey = -1;
+  CT zc = CT(0);
+  int carry_key = -1;  // the open group segment (thread my_rl == 0 of each chain)
+  CT carry_val = CT(0);
+  auto put_gz = [&](int key, CT v) { Gz[(size_t)cg * m.J + key] = (double)v; };
+
+  for (long long r0 = row_begin; r0 < row_end; r0 += RB) {
+    const int nrows = (int)min((long long)RB, row_end - r0);
+    __syncthreads();
+    // the tile's rows are contiguous in X: element idx = r K + k, stepped
+    // by kThreads = dr K + dk without a division per element
+    const XT* xt = X + (size_t)r0 * K;
+    {
+      int r = tid / K, k = tid - (tid / K) * K;
+      for (int idx = tid; idx < nrows * K; idx += kThreads) {
+        x_s[r * KS + k] = x_to<CT, XT>(xt[idx]);
+        r += dr;
+        k += dk;
+        if (k >= K) {
+          k -= K;
+          ++r;
+        }
+      }
+    }
+    for (int idx = tid; idx < RB; idx += kThreads) {
+      y_s[idx] = idx < nrows ? (CT)m.y[r0 + idx] : CT(0);
+      g_s[idx] = (has_z && idx < nrows) ? m.group[r0 + idx] : -1;
+    }
+    __syncthreads();
+
+    CT lp_t = 0, base_t = 0, tau_t = 0, sq_t = 0;
+    int fkey = -2, ckey = -2;  // first closed segment's group, current segment's
+    CT fsum = CT(0), cur = CT(0);
+    const int rb0 = my_rl * RR;
+    if (cact) {
+      for (int j = 0; j < RR; ++j) {
+        const int r = rb0 + j;
+        if (r >= nrows) break;
+        CT xr[SK];
+#pragma unroll
+        for (int k = 0; k < SK; k += VW) {
+          if (k < KS) {
+            if (VW == 4) {
+              const float4 v = *reinterpret_cast<const float4*>(x_s + r * KS + k);
+              xr[k] = v.x;
+              xr[k + 1] = v.y;
+              xr[k + 2] = v.z;
+              xr[k + 3] = v.w;
+            } else {
+              const double2 v = *reinterpret_cast<const double2*>(x_s + r * KS + k);
+              xr[k] = v.x;
+              xr[k + 1] = v.y;
+            }
+          } else {
+#pragma unroll
+            for (int u = 0; u < VW; ++u) xr[k + u] = CT(0);
+          }
+        }
+        CT dotv = CT(0);
+#pragma unroll
+        for (int k = 0; k < SK; ++k) dotv = fma(xr[k], th[k], dotv);
+        CT eta = base + dotv;
+        const int g = g_s[r];
+        if (has_z) {
+          if (g != zkey) {
+            zkey = g;
+            zc = (CT)thq[m.off_z + g];
+          }
+          eta += tau * zc;
+        }
+        CT term, resid, sq;
+        apply_link<CT>(m.link, eta, y_s[r], invs2, term, resid, sq);
+        lp_t += term;
+        base_t += resid;
+        tau_t += resid * zc;
+        sq_t += sq;
+#pragma unroll
+        for (int k = 0; k < SK; ++k) acc[k] = fma(xr[k], resid, acc[k]);
+        if (has_z) {
+          if (g != ckey) {
+            if (ckey >= 0) {
+              if (fkey == -2) {
+                fkey = ckey;
+                fsum = cur;
+              } else {
+                put_gz(ckey, cur);  // a segment inside the run
+              }
+            }
+            ckey = g;
+            cur = CT(0);
+          }
+          cur += resid;
+        }
+      }
+    }
+    lp_d += (double)lp_t;
+    base_d += (double)base_t;
+    tau_d += (double)tau_t;
+    sq_d += (double)sq_t;
+    if (has_z) {
+      // the run's first closed segment (or -2: one segment) and its last one
+      RunEnds* ends = reinterpret_cast<RunEnds*>(red_s);
+      ends[tid] = RunEnds{fkey, ckey, fsum, cur};
+      __syncthreads();
+      if (my_rl == 0 && cact) {
+        for (int rl = 0; rl < RPT; ++rl) {
+          const RunEnds e = ends[rl * CB + my_c];
+          const int fk = e.fkey, lk = e.lkey;
+          if (lk < 0) continue;  // no rows
+          const CT fs = e.fsum, ls = e.lsum;
+          if (fk >= 0) {
+            // two or more segments: the first one ends inside this run
+            if (fk == carry_key) {
+              carry_val += fs;
+            } else {
+              if (carry_key >= 0) put_gz(carry_key, carry_val);
+              carry_val = fs;
+            }
+            put_gz(fk, carry_val);
+            carry_key = lk;
+            carry_val = ls;
+          } else if (lk == carry_key) {
+            carry_val += ls;
+          } else {
+            if (carry_key >= 0) put_gz(carry_key, carry_val);
+            carry_key = lk;
+            carry_val = ls;
+          }
+        }
+      }
+    }
+  }
+  if (has_z && my_rl == 0 && cact && carry_key >= 0) put_gz(carry_key, carry_val);
+
+  // X^T r: the runs' sums of each (chain, feature) added in run order
+  __syncthreads();
+  CT* red = x_s;  // [RPT][CB][K], fits in the tile's rows (RB KS >= RPT CB K)
+#pragma unroll
+  for (int k = 0; k < SK; ++k)
+    if (k < K) red[(size_t)tid * K + k] = acc[k];
+  __syncthreads();
+  for (int p = tid; p < CB * K; p += kThreads) {
+    const int c = p / K, k = p - c * K;
+    if (!act_s[c]) continue;
+    double a = 0;
+    for (int rl = 0; rl < RPT; ++rl) a += (double)red[(size_t)(rl * CB + c) * K + k];
+    P[((size_t)s * C + c0 + c) * NP + 4 + k] = a;
+  }
 }
 
 // One CTA's work: split s of the rows, chain block cb (CB chains), RB rows per
@@ -136,142 +368,148 @@ __device__ __forceinline__ void loglik_partial_body(
   const int warp = tid >> 5, lane = tid & 31;
   const bool has_z = m.off_z >= 0;
   double lp_d = 0, base_d = 0, tau_d = 0, sq_d = 0;
-  CT acc[kMaxPairs];
+  if (use_small_k<CT>(K)) {  // RB >= kThreads, whole runs of rows (choose_rb)
+    small_k_rows<XT, CT, CB>(m, Q, ldq, C, th_s, base_s, tau_s, invs2_s, act_s, red_s, RB,
+                             row_begin, row_end, P, NP, Gz, s, c0, lp_d, base_d, tau_d,
+                             sq_d);
+  } else {
+    CT acc[kMaxPairs];
 #pragma unroll
-  for (int j = 0; j < kMaxPairs; ++j) acc[j] = CT(0);
-  // segmented-scan carry for the group sums, per (warp, chain slot)
-  constexpr int kChainsPerWarp = (CB + 7) / 8;
-  int carry_key[kChainsPerWarp];
-  CT carry_val[kChainsPerWarp];
+    for (int j = 0; j < kMaxPairs; ++j) acc[j] = CT(0);
+    // segmented-scan carry for the group sums, per (warp, chain slot)
+    constexpr int kChainsPerWarp = (CB + 7) / 8;
+    int carry_key[kChainsPerWarp];
+    CT carry_val[kChainsPerWarp];
 #pragma unroll
-  for (int i = 0; i < kChainsPerWarp; ++i) {
-    carry_key[i] = -1;
-    carry_val[i] = CT(0);
-  }
-
-  for (long long r0 = row_begin; r0 < row_end; r0 += RB) {
-    const int nrows = (int)min((long long)RB, row_end - r0);
-    __syncthreads();
-    const XT* xt = X + (size_t)r0 * K;
-    for (int idx = tid; idx < nrows * K; idx += kThreads) {
-      int r = idx / K, k = idx - r * K;
-      x_s[r * KP + k] = (CT)x_to_double<XT>(xt[idx]);
+    for (int i = 0; i < kChainsPerWarp; ++i) {
+      carry_key[i] = -1;
+      carry_val[i] = CT(0);
     }
-    for (int idx = tid; idx < RB; idx += kThreads) {
-      y_s[idx] = idx < nrows ? (CT)m.y[r0 + idx] : CT(0);
-      g_s[idx] = (has_z && idx < nrows) ? m.group[r0 + idx] : -1;
-    }
-    __syncthreads();
 
-    // forward: eta, link, per-chain scalar sums
-    {
-      CT lp_t = 0, base_t = 0, tau_t = 0, sq_t = 0;
-      const bool cact = act_s[my_c] != 0;
-      const CT* tc = th_s + my_c * KP;
-      const double* thq = Q + (size_t)(c0 + my_c) * ldq;
-      for (int r = my_rl; r < RB; r += RPT) {
-        CT resid = CT(0);
-        if (cact && r < nrows) {
-          const CT* xr = x_s + r * KP;
-          CT dotv = CT(0);
-          for (int k = 0; k < K; ++k) dotv = fma(xr[k], tc[k], dotv);
-          CT eta = base_s[my_c] + dotv;
-          CT zg = CT(0);
-          if (has_z) {
-            zg = (CT)thq[m.off_z + g_s[r]];
-            eta += tau_s[my_c] * zg;
-          }
-          CT term, sq;
-          apply_link<CT>(m.link, eta, y_s[r], invs2_s[my_c], term, resid, sq);
-          lp_t += term;
-          base_t += resid;
-          tau_t += resid * zg;
-          sq_t += sq;
-        }
-        r_s[r * CB + my_c] = resid;
+    for (long long r0 = row_begin; r0 < row_end; r0 += RB) {
+      const int nrows = (int)min((long long)RB, row_end - r0);
+      __syncthreads();
+      const XT* xt = X + (size_t)r0 * K;
+      for (int idx = tid; idx < nrows * K; idx += kThreads) {
+        int r = idx / K, k = idx - r * K;
+        x_s[r * KP + k] = x_to<CT, XT>(xt[idx]);
       }
-      lp_d += (double)lp_t;
-      base_d += (double)base_t;
-      tau_d += (double)tau_t;
-      sq_d += (double)sq_t;
-    }
-    __syncthreads();
+      for (int idx = tid; idx < RB; idx += kThreads) {
+        y_s[idx] = idx < nrows ? (CT)m.y[r0 + idx] : CT(0);
+        g_s[idx] = (has_z && idx < nrows) ? m.group[r0 + idx] : -1;
+      }
+      __syncthreads();
 
-    // adjoint: X^T r for (chain, feature) pairs
+      // forward: eta, link, per-chain scalar sums
+      {
+        CT lp_t = 0, base_t = 0, tau_t = 0, sq_t = 0;
+        const bool cact = act_s[my_c] != 0;
+        const CT* tc = th_s + my_c * KP;
+        const double* thq = Q + (size_t)(c0 + my_c) * ldq;
+        for (int r = my_rl; r < RB; r += RPT) {
+          CT resid = CT(0);
+          if (cact && r < nrows) {
+            const CT* xr = x_s + r * KP;
+            CT dotv = CT(0);
+            for (int k = 0; k < K; ++k) dotv = fma(xr[k], tc[k], dotv);
+            CT eta = base_s[my_c] + dotv;
+            CT zg = CT(0);
+            if (has_z) {
+              zg = (CT)thq[m.off_z + g_s[r]];
+              eta += tau_s[my_c] * zg;
+            }
+            CT term, sq;
+            apply_link<CT>(m.link, eta, y_s[r], invs2_s[my_c], term, resid, sq);
+            lp_t += term;
+            base_t += resid;
+            tau_t += resid * zg;
+            sq_t += sq;
+          }
+          r_s[r * CB + my_c] = resid;
+        }
+        lp_d += (double)lp_t;
+        base_d += (double)base_t;
+        tau_d += (double)tau_t;
+        sq_d += (double)sq_t;
+      }
+      __syncthreads();
+
+      // adjoint: X^T r for (chain, feature) pairs
+#pragma unroll
+      for (int j = 0; j < kMaxPairs; ++j) {
+        int p = tid + kThreads * j;
+        if (p < CB * K) {
+          int c = p / K, k = p - c * K;
+          CT a = CT(0);
+          for (int r = 0; r < nrows; ++r) a = fma(x_s[r * KP + k], r_s[r * CB + c], a);
+          acc[j] += a;
+        }
+      }
+
+      // group sums: warp w handles chain slots w, w + 8, ...
+      if (has_z) {
+#pragma unroll
+        for (int i = 0; i < kChainsPerWarp; ++i) {
+          const int c = warp + 8 * i;
+          if (c < CB && act_s[c]) {
+            const int cg = c0 + c;
+            for (int rb = 0; rb < nrows; rb += 32) {
+              const int r = rb + lane;
+              int key = r < nrows ? g_s[r] : -2 - lane;
+              CT val = r < nrows ? r_s[r * CB + c] : CT(0);
+#pragma unroll
+              for (int off = 1; off < 32; off <<= 1) {
+                CT v = __shfl_up_sync(0xffffffffu, val, off);
+                int kk = __shfl_up_sync(0xffffffffu, key, off);
+                if (lane >= off && kk == key) val += v;
+              }
+              int next_key = __shfl_down_sync(0xffffffffu, key, 1);
+              bool seg_end = (lane == 31) || (next_key != key);
+              // the first segment of the chunk continues the carried one
+              int first_key = __shfl_sync(0xffffffffu, key, 0);
+              if (key == first_key && key == carry_key[i]) val += carry_val[i];
+              int last_key = __shfl_sync(0xffffffffu, key, 31);
+              CT last_val = __shfl_sync(0xffffffffu, val, 31);
+              if (seg_end && r < nrows && lane != 31) Gz[(size_t)cg * m.J + key] = (double)val;
+              // the chunk's last segment may continue into the next chunk
+              if (last_key >= 0) {
+                if (carry_key[i] >= 0 && carry_key[i] != first_key && lane == 0) {
+                  // carried segment ended exactly at the previous chunk boundary
+                  Gz[(size_t)cg * m.J + carry_key[i]] = (double)carry_val[i];
+                }
+                carry_key[i] = last_key;
+                carry_val[i] = last_val;
+              } else {
+                // partial chunk ending the tile: last valid lane closes its segment
+                // (it was written above unless it is lane 31, impossible here)
+                if (carry_key[i] >= 0 && carry_key[i] != first_key && lane == 0)
+                  Gz[(size_t)cg * m.J + carry_key[i]] = (double)carry_val[i];
+                carry_key[i] = -1;
+                carry_val[i] = CT(0);
+              }
+            }
+          }
+        }
+      }
+    }
+
+    // flush open group segments
+    if (has_z && lane == 0) {
+#pragma unroll
+      for (int i = 0; i < kChainsPerWarp; ++i) {
+        const int c = warp + 8 * i;
+        if (c < CB && act_s[c] && carry_key[i] >= 0)
+          Gz[(size_t)(c0 + c) * m.J + carry_key[i]] = (double)carry_val[i];
+      }
+    }
+
 #pragma unroll
     for (int j = 0; j < kMaxPairs; ++j) {
       int p = tid + kThreads * j;
       if (p < CB * K) {
         int c = p / K, k = p - c * K;
-        CT a = CT(0);
-        for (int r = 0; r < nrows; ++r) a = fma(x_s[r * KP + k], r_s[r * CB + c], a);
-        acc[j] += a;
+        if (act_s[c]) P[((size_t)s * C + c0 + c) * NP + 4 + k] = (double)acc[j];
       }
-    }
-
-    // group sums: warp w handles chain slots w, w + 8, ...
-    if (has_z) {
-#pragma unroll
-      for (int i = 0; i < kChainsPerWarp; ++i) {
-        const int c = warp + 8 * i;
-        if (c < CB && act_s[c]) {
-          const int cg = c0 + c;
-          for (int rb = 0; rb < nrows; rb += 32) {
-            const int r = rb + lane;
-            int key = r < nrows ? g_s[r] : -2 - lane;
-            CT val = r < nrows ? r_s[r * CB + c] : CT(0);
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-              CT v = __shfl_up_sync(0xffffffffu, val, off);
-              int kk = __shfl_up_sync(0xffffffffu, key, off);
-              if (lane >= off && kk == key) val += v;
-            }
-            int next_key = __shfl_down_sync(0xffffffffu, key, 1);
-            bool seg_end = (lane == 31) || (next_key != key);
-            // the first segment of the chunk continues the carried one
-            int first_key = __shfl_sync(0xffffffffu, key, 0);
-            if (key == first_key && key == carry_key[i]) val += carry_val[i];
-            int last_key = __shfl_sync(0xffffffffu, key, 31);
-            CT last_val = __shfl_sync(0xffffffffu, val, 31);
-            if (seg_end && r < nrows && lane != 31) Gz[(size_t)cg * m.J + key] = (double)val;
-            // the chunk's last segment may continue into the next chunk
-            if (last_key >= 0) {
-              if (carry_key[i] >= 0 && carry_key[i] != first_key && lane == 0) {
-                // carried segment ended exactly at the previous chunk boundary
-                Gz[(size_t)cg * m.J + carry_key[i]] = (double)carry_val[i];
-              }
-              carry_key[i] = last_key;
-              carry_val[i] = last_val;
-            } else {
-              // partial chunk ending the tile: last valid lane closes its segment
-              // (it was written above unless it is lane 31, impossible here)
-              if (carry_key[i] >= 0 && carry_key[i] != first_key && lane == 0)
-                Gz[(size_t)cg * m.J + carry_key[i]] = (double)carry_val[i];
-              carry_key[i] = -1;
-              carry_val[i] = CT(0);
-            }
-          }
-        }
-      }
-    }
-  }
-
-  // flush open group segments
-  if (has_z && lane == 0) {
-#pragma unroll
-    for (int i = 0; i < kChainsPerWarp; ++i) {
-      const int c = warp + 8 * i;
-      if (c < CB && act_s[c] && carry_key[i] >= 0)
-        Gz[(size_t)(c0 + c) * m.J + carry_key[i]] = (double)carry_val[i];
-    }
-  }
-
-#pragma unroll
-  for (int j = 0; j < kMaxPairs; ++j) {
-    int p = tid + kThreads * j;
-    if (p < CB * K) {
-      int c = p / K, k = p - c * K;
-      if (act_s[c]) P[((size_t)s * C + c0 + c) * NP + 4 + k] = (double)acc[j];
     }
   }
   red_s[tid][0] = lp_d;
@@ -339,6 +577,16 @@ static constexpr size_t kSmemBudget = 150 * 1024;
 
 template <typename CT>
 static int choose_rb(int CB, int K) {
+  if (use_small_k<CT>(K)) {
+    // whole runs of rows per thread: RB = RPT x rows per run, at least one
+    // row per thread (RB >= kThreads: the runs' adjoint sums reuse the rows'
+    // space), at most kSmallRunRows rows per run and ~kSmallTileBytes
+    const int rpt = kThreads / CB;
+    const size_t row_bytes = sizeof(CT) * (small_row_stride<CT>(K) + 1) + sizeof(int);
+    int rr = (int)std::min<size_t>(kSmallRunRows, kSmallTileBytes / (row_bytes * rpt));
+    rr = std::max(rr, (kThreads + rpt - 1) / rpt);
+    return rr * rpt;
+  }
   int rb = 256;
   while (rb > 32 && partial_smem_bytes<CT>(CB, K, rb) > kSmemBudget) rb -= 32;
   return rb;

@@ -80,26 +80,36 @@ def test_full_size_logistic_batch():
         assert np.linalg.norm(g32[c] - go) <= 1e-4 * np.linalg.norm(go)
 
 
-def test_group_sums_with_single_row_groups_and_large_groups():
-    """Segmented group reduction across tile and chunk boundaries."""
+@pytest.mark.parametrize("K", [3, 16, 17])
+@pytest.mark.parametrize("C", [3, 5, 20])
+def test_group_sums_with_single_row_groups_and_large_groups(K, C):
+    """Segmented group reduction across tile, run and chunk boundaries: groups
+    of one row, an empty group, groups longer than a tile; chain blocks of 4,
+    8 and 16 chains; up to 16 features the per-thread row runs, above that
+    the general form."""
     from stan_gb300 import Model
     from stan_gb300.workloads import Dataset, HIER_NORMAL
-    rng = np.random.default_rng(5)
-    sizes = np.array([1, 1, 300, 2, 31, 32, 33, 64, 65, 1, 500, 7])
+    rng = np.random.default_rng(5 + K + C)
+    sizes = np.array([1, 1, 300, 2, 31, 32, 33, 0, 64, 65, 1, 500, 7, 16, 15, 17, 1, 1, 260])
     J = sizes.size
     g = np.repeat(np.arange(J, dtype=np.int32), sizes)
-    N, K = g.size, 3
+    N = g.size
     X = rng.normal(size=(N, K))
     y = rng.normal(size=N)
     ds = Dataset("groups", HIER_NORMAL, X, y, "f64", group=g, J=J, hp=(5.0, 1.0, 1.0, 1.0))
     m = Model.from_dataset(ds)
     om = ds.oracle_model()
-    th = _points(m.D, 5, 6)
+    th = _points(m.D, C, 6)
     lp, gr = m.log_prob_grad_batch(th, "fp64")
-    for c in range(5):
+    lp32, gr32 = m.log_prob_grad_batch(th, "fp32")
+    for c in range(C):
         lpo, go = om.log_prob_grad(th[c])
         assert abs(lp[c] - lpo) <= 1e-12 * abs(lpo)
         assert np.max(np.abs(gr[c] - go)) <= 1e-12 * np.max(np.abs(go))
+        assert abs(lp32[c] - lpo) <= 1e-5 * abs(lpo)
+        assert np.linalg.norm(gr32[c] - go) <= 1e-4 * np.linalg.norm(go)
+    lp2, gr2 = m.log_prob_grad_batch(th, "fp32")
+    assert np.array_equal(lp2, lp32) and np.array_equal(gr2, gr32)  # deterministic
 
 
 def test_non_finite_density_is_reported_not_raised(models):
