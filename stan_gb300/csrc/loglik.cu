@@ -120,7 +120,7 @@ __host__ __device__ inline size_t partial_smem_bytes(int CB, int K, int RB) {
 
 // Designs of up to small_k_max<CT>() features (the hierarchical models'
 // group-level predictors): each thread owns one chain and a contiguous run of
-// RR = RB / RPT rows of every tile.  Theta, the K adjoint sums and the z of
+// RR <= RB / RPT rows of every tile.  Theta, the K adjoint sums and the z of
 // the current group stay in registers (z is re-read and converted only when
 // the group changes); a row's features are 16-byte loads from shared memory,
 // and eta, the link and the adjoint update X^T r run in one pass over the row.
@@ -141,7 +141,14 @@ __device__ __forceinline__ void small_k_rows(
   constexpr int RPT = kThreads / CB;    // runs (threads) per chain
   const int K = m.K, KP = K + 1;
   const int KS = (K + VW - 1) / VW * VW;
-  const int RR = RB / RPT;
+  // rows per run: at most RB / RPT, and the split's rows in tiles of equal
+  // size, so every run of every tile has rows (a short split or a short
+  // last tile would otherwise leave most runs idle)
+  const long long n_split = row_end - row_begin;
+  const long long cap = (long long)(RB / RPT) * RPT;
+  const long long n_tiles = (n_split + cap - 1) / cap;
+  const int RR = n_tiles > 0 ? (int)((n_split + n_tiles * RPT - 1) / (n_tiles * RPT)) : 1;
+  const int RBe = RR * RPT;  // rows per tile (<= RB)
   const int dr = kThreads / K, dk = kThreads - (kThreads / K) * K;
   const int tid = threadIdx.x, my_c = tid % CB, my_rl = tid / CB;
   CT* x_s = const_cast<CT*>(th_s) + (size_t)CB * KP;  // [RB][KS]
@@ -177,8 +184,8 @@ __device__ __forceinline__ void small_k_rows(
   CT carry_val = CT(0);
   auto put_gz = [&](int key, CT v) { Gz[(size_t)cg * m.J + key] = (double)v; };
 
-  for (long long r0 = row_begin; r0 < row_end; r0 += RB) {
-    const int nrows = (int)min((long long)RB, row_end - r0);
+  for (long long r0 = row_begin; r0 < row_end; r0 += RBe) {
+    const int nrows = (int)min((long long)RBe, row_end - r0);
     __syncthreads();
     // the tile's rows are contiguous in X: element idx = r K + k, stepped
     // by kThreads = dr K + dk without a division per element
@@ -195,7 +202,7 @@ __device__ __forceinline__ void small_k_rows(
         }
       }
     }
-    for (int idx = tid; idx < RB; idx += kThreads) {
+    for (int idx = tid; idx < RBe; idx += kThreads) {
       y_s[idx] = idx < nrows ? (CT)m.y[r0 + idx] : CT(0);
       g_s[idx] = (has_z && idx < nrows) ? m.group[r0 + idx] : -1;
     }
